@@ -1,0 +1,320 @@
+"""numpy front end of the CPU oracle (test infrastructure only).
+
+Mirrors the reference's Python-level ops (``pystrns2cards/{dda,rasterize,antialias,
+bitset_utils,curve_utils}.py``) on numpy arrays over ``liboracle.so`` (s2c_oracle.c).
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+i32p = ctypes.POINTER(ctypes.c_int32)
+f32p = ctypes.POINTER(ctypes.c_float)
+f64p = ctypes.POINTER(ctypes.c_double)
+I64 = ctypes.c_int64
+I = ctypes.c_int
+F = ctypes.c_float
+
+_SIGS = {
+    "or_version": ([], I),
+    "or_set_model": ([I], None),
+    "or_get_model": ([], I),
+    "or_set_threads": ([I], None),
+    "or_dda_span": ([I64, i32p, I, I, I, f32p, I, i32p, i32p, f32p, f32p], None),
+    "or_dda_fragments": ([I64, i32p, i32p, f32p, f32p, I, I, I, f32p, I, i32p, i32p, f32p], None),
+    "or_dda_cluster_bitset": ([I, I, I, I, f32p, I, i32p, i32p, I64, i32p, I, i32p], None),
+    "or_tri_rects": ([I, I, I, I, f32p, I, i32p, i32p, i32p], None),
+    "or_tri_fragments": ([I, I, I, I, f32p, I, i32p, i32p, i32p, i32p, f32p], None),
+    "or_filter_valid": ([I64, i32p, f32p, i32p, f32p], I64),
+    "or_depth_test": ([I, I, I, I64, i32p, f32p, f32p], None),
+    "or_cluster_mask": ([I64, i32p, f32p, i32p, I, I, I, i32p], None),
+    "or_interpolate": ([I, I, I, f32p, I, f32p, i32p, f64p], None),
+    "or_interpolate_backward": ([I, I, I, f32p, I, f32p, i32p, f64p], None),
+    "or_dda_interpolate": ([I, I, I, f32p, I, f32p, i32p, f64p], None),
+    "or_dda_interpolate_backward": ([I, I, I, f32p, I, f32p, i32p, f64p], None),
+    "or_mark_edges": ([I, I, I, I, f32p, i32p, I, i32p, i32p, i32p, f32p], None),
+    "or_compact_ints": ([I64, i32p, i32p], I64),
+    "or_aa_backward": ([I64, i32p, f32p, I, I, I, i32p, i32p, I, f32p, I, i32p, f32p, i32p, f64p, F, F], None),
+    "or_popcount": ([I64, I, i32p, f32p], None),
+    "or_accumulate_rgb": ([I64, I, i32p, f32p, f32p], None),
+    "or_smooth_strands": ([I, I, f32p, f32p, f64p, F], None),
+    "or_skinning": ([I, I, f32p, f32p, f32p, f32p, f32p, f64p, F], None),
+}
+
+# arithmetic-model flags (s2c_oracle.h)
+FMA_DDA_SPAN, FMA_DDA_STEP, FMA_DDA_PERSP, FMA_DDA_Z = 1, 2, 4, 8
+FMA_TRI_RECT, FMA_TRI_Q, FMA_TRI_A, FMA_TRI_A_ALT, FMA_TRI_Z, FMA_AA = 16, 32, 64, 128, 256, 512
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        src = os.path.join(HERE, "s2c_oracle.c")
+        if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            subprocess.run(["make", "-s", "-C", HERE], check=True)
+        L = ctypes.CDLL(path)
+        for name, (args, res) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _LIB = L
+    return _LIB
+
+
+def _p(a: Optional[np.ndarray], ptype):
+    if a is None:
+        return ctypes.cast(None, ptype)
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be contiguous"
+    return a.ctypes.data_as(ptype)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def set_model(flags: int = -1):
+    lib().or_set_model(int(flags))
+
+
+def get_model() -> int:
+    return int(lib().or_get_model())
+
+
+def set_threads(n: int):
+    lib().or_set_threads(int(n))
+
+
+# ---- dda.py ------------------------------------------------------------------------
+def dda_span(H, W, pos, edges, edge_ids=None):
+    pos, edges = _f32(pos), _i32(edges)
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    ids = None if edge_ids is None else _i32(edge_ids)
+    P = B * E if ids is None else ids.shape[0]
+    counts = np.empty(P, np.int32)
+    slopes = np.empty((P, 2), np.float32)
+    spans = np.empty((P, 4), np.float32)
+    lib().or_dda_span(P, _p(ids, i32p), H, W, V, _p(pos, f32p), E, _p(edges, i32p),
+                      _p(counts, i32p), _p(slopes, f32p), _p(spans, f32p))
+    return counts, slopes, spans
+
+
+def dda_compute_fragments(H, W, pos, edges, edge_ids=None, raw=False):
+    """``dda.py:5-76``; fragments in prim order (the order an in-order compaction gives)."""
+    pos, edges = _f32(pos), _i32(edges)
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    ids = None if edge_ids is None else _i32(edge_ids)
+    counts, slopes, spans = dda_span(H, W, pos, edges, ids)
+    prefix = np.cumsum(counts, dtype=np.int64).astype(np.int32)
+    Ft = int(prefix[-1]) if prefix.shape[0] else 0
+    pix = np.full((Ft, 3), -1, np.int32)
+    attrs = np.zeros((Ft, 4), np.float32)
+    lib().or_dda_fragments(counts.shape[0], _p(prefix, i32p), _p(ids, i32p), _p(slopes, f32p),
+                           _p(spans, f32p), H, W, V, _p(pos, f32p), E, _p(edges, i32p),
+                           _p(pix, i32p), _p(attrs, f32p))
+    po = np.empty_like(pix)
+    ao = np.empty_like(attrs)
+    n = lib().or_filter_valid(Ft, _p(pix, i32p), _p(attrs, f32p), _p(po, i32p), _p(ao, f32p))
+    if raw:
+        return po[:n], ao[:n], dict(counts=counts, slopes=slopes, spans=spans, prefix=prefix,
+                                    raw_pix=pix, raw_attrs=attrs)
+    return po[:n], ao[:n]
+
+
+def dda_cluster_bitset(H, W, pos, edges, prim2cluster, K, edge_ids=None):
+    pos, edges, p2c = _f32(pos), _i32(edges), _i32(prim2cluster)
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    S = (K + 31) // 32
+    ids = None if edge_ids is None else _i32(edge_ids)
+    P = B * E if ids is None else ids.shape[0]
+    bits = np.empty((B, H, W, S), np.int32)
+    lib().or_dda_cluster_bitset(B, H, W, V, _p(pos, f32p), E, _p(edges, i32p), _p(ids, i32p), P,
+                                _p(p2c, i32p), S, _p(bits, i32p))
+    return bits
+
+
+def cluster_mask_from_fragments(H, W, frag_pix, frag_attrs, prim2cluster, cluster_count=None, B=None):
+    """``rasterize.py:170-214`` (B inferred from the fragments unless given)."""
+    fp, fa, p2c = _i32(frag_pix), _f32(frag_attrs), _i32(prim2cluster)
+    if B is None:
+        B = int(fp[:, 0].max()) + 1
+    K = cluster_count if cluster_count is not None else int(p2c.max()) + 1
+    S = (K + 31) // 32
+    bits = np.zeros((B, H, W, S), np.int32)
+    lib().or_cluster_mask(fp.shape[0], _p(fp, i32p), _p(fa, f32p), _p(p2c, i32p), H, W, S, _p(bits, i32p))
+    return bits
+
+
+# ---- rasterize.py --------------------------------------------------------------------
+def tri_rects(H, W, pos, tri):
+    pos, tri = _f32(pos), _i32(tri)
+    B, V, _ = pos.shape
+    T = tri.shape[0]
+    rects = np.empty((B * T, 4), np.int32)
+    counts = np.empty(B * T, np.int32)
+    lib().or_tri_rects(H, W, B, V, _p(pos, f32p), T, _p(tri, i32p), _p(rects, i32p), _p(counts, i32p))
+    return rects, counts
+
+
+def compute_fragments(H, W, pos, tri, raw=False):
+    """``rasterize.py:6-53``; fragments in (view, triangle, row-major pixel) order."""
+    pos, tri = _f32(pos), _i32(tri)
+    B, V, _ = pos.shape
+    T = tri.shape[0]
+    rects, counts = tri_rects(H, W, pos, tri)
+    prefix = np.cumsum(counts, dtype=np.int64).astype(np.int32)
+    Ft = int(prefix[-1]) if prefix.shape[0] else 0
+    pix = np.full((Ft, 3), -1, np.int32)
+    attrs = np.zeros((Ft, 4), np.float32)
+    lib().or_tri_fragments(H, W, B, V, _p(pos, f32p), T, _p(tri, i32p), _p(rects, i32p),
+                           _p(prefix, i32p), _p(pix, i32p), _p(attrs, f32p))
+    po = np.empty_like(pix)
+    ao = np.empty_like(attrs)
+    n = lib().or_filter_valid(Ft, _p(pix, i32p), _p(attrs, f32p), _p(po, i32p), _p(ao, f32p))
+    if raw:
+        return po[:n], ao[:n], dict(rects=rects, counts=counts)
+    return po[:n], ao[:n]
+
+
+def depth_test(B, H, W, frag_pix, frag_attrs):
+    fp, fa = _i32(frag_pix), _f32(frag_attrs)
+    rast = np.empty((B, H, W, 4), np.float32)
+    lib().or_depth_test(B, H, W, fp.shape[0], _p(fp, i32p), _p(fa, f32p), _p(rast, f32p))
+    return rast
+
+
+def rasterize(H, W, pos, tri):
+    fp, fa = compute_fragments(H, W, pos, tri)
+    return depth_test(pos.shape[0], H, W, fp, fa)
+
+
+def interpolate(rast, attr, tri):
+    rast, attr, tri = _f32(rast), _f32(attr), _i32(tri)
+    B, H, W, _ = rast.shape
+    C = attr.shape[1]
+    img = np.empty((B, H, W, C), np.float64)
+    lib().or_interpolate(B, H, W, _p(rast, f32p), C, _p(attr, f32p), _p(tri, i32p), _p(img, f64p))
+    return img
+
+
+def interpolate_backward(rast, d_image, tri, V):
+    rast, g, tri = _f32(rast), _f32(d_image), _i32(tri)
+    B, H, W, _ = rast.shape
+    C = g.shape[3]
+    d = np.zeros((V, C), np.float64)
+    lib().or_interpolate_backward(B, H, W, _p(rast, f32p), C, _p(g, f32p), _p(tri, i32p), _p(d, f64p))
+    return d
+
+
+def dda_interpolate(rast, attr, edges):
+    rast, attr, edges = _f32(rast), _f32(attr), _i32(edges)
+    B, H, W, _ = rast.shape
+    C = attr.shape[1]
+    img = np.empty((B, H, W, C), np.float64)
+    lib().or_dda_interpolate(B, H, W, _p(rast, f32p), C, _p(attr, f32p), _p(edges, i32p), _p(img, f64p))
+    return img
+
+
+def dda_interpolate_backward(rast, d_image, edges, V):
+    rast, g, edges = _f32(rast), _f32(d_image), _i32(edges)
+    B, H, W, _ = rast.shape
+    C = g.shape[3]
+    d = np.zeros((V, C), np.float64)
+    lib().or_dda_interpolate_backward(B, H, W, _p(rast, f32p), C, _p(g, f32p), _p(edges, i32p), _p(d, f64p))
+    return d
+
+
+# ---- antialias.py --------------------------------------------------------------------
+def mark_discontinuity_edges(H, W, pos, tri, edges, edge2tri, raw=False):
+    """``antialias.py:8-52``: (compacted prim ids in index order, normals (B*E, 2))."""
+    pos, tri, edges, e2t = _f32(pos), _i32(tri), _i32(edges), _i32(edge2tri)
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    ids = np.full(B * E, -1, np.int32)
+    normals = np.zeros((B * E, 2), np.float32)
+    lib().or_mark_edges(H, W, B, V, _p(pos, f32p), _p(tri, i32p), E, _p(edges, i32p), _p(e2t, i32p),
+                        _p(ids, i32p), _p(normals, f32p))
+    out = np.empty_like(ids)
+    n = lib().or_compact_ints(ids.shape[0], _p(ids, i32p), _p(out, i32p))
+    if raw:
+        return out[:n], normals, ids
+    return out[:n], normals
+
+
+def aa_backward(frag_pix, frag_attrs, bitset, target, pos, edges, normals, edge2cluster,
+                kernel_radius=7.0, rho=1.0):
+    fp, fa = _i32(frag_pix), _f32(frag_attrs)
+    bits, tgt = _i32(bitset), _i32(target)
+    pos, edges, normals, e2c = _f32(pos), _i32(edges), _f32(normals), _i32(edge2cluster)
+    B, H, W, S = bits.shape
+    V = pos.shape[1]
+    E = edges.shape[0]
+    d = np.zeros(pos.shape, np.float64)
+    lib().or_aa_backward(fp.shape[0], _p(fp, i32p), _p(fa, f32p), H, W, S, _p(bits, i32p), _p(tgt, i32p),
+                         V, _p(pos, f32p), E, _p(edges, i32p), _p(normals, f32p), _p(e2c, i32p),
+                         _p(d, f64p), float(kernel_radius), float(rho))
+    return d
+
+
+def antialias_grad(bitset, target, pos, tri, edges, edge2tri, edge2cluster, kernel_radius=7.0, rho=1.0):
+    """``antialias.py:66-130`` up to ``d_pos`` (FP64)."""
+    _, H, W, _ = target.shape
+    ids, normals = mark_discontinuity_edges(H, W, pos, tri, edges, edge2tri)
+    fp, fa = dda_compute_fragments(H, W, pos, edges, ids)
+    return aa_backward(fp, fa, bitset, target, pos, edges, normals, edge2cluster, kernel_radius, rho)
+
+
+# ---- bitset_utils.py -----------------------------------------------------------------
+def popcount_bitset(bitset):
+    b = _i32(bitset)
+    out = np.empty(b.shape[:3], np.float32)
+    lib().or_popcount(int(np.prod(b.shape[:3])), b.shape[3], _p(b, i32p), _p(out, f32p))
+    return out
+
+
+def accumulate_bitset_rgb(bitset, rgb):
+    b, c = _i32(bitset), _f32(rgb)
+    out = np.empty(b.shape[:3] + (3,), np.float32)
+    lib().or_accumulate_rgb(int(np.prod(b.shape[:3])), b.shape[3], _p(b, i32p), _p(c, f32p), _p(out, f32p))
+    return out
+
+
+# ---- curve_utils.py ------------------------------------------------------------------
+def smooth_strands(strands, arclength, beta):
+    s, a = _f32(strands), _f32(arclength)
+    N, V, _ = s.shape
+    out = np.zeros(s.shape, np.float64)
+    lib().or_smooth_strands(N, V, _p(s, f32p), _p(a, f32p), _p(out, f64p), float(beta))
+    return out
+
+
+def skinning(strands, arclength, handles, canonical, R, beta):
+    s, a, h, c, r = _f32(strands), _f32(arclength), _f32(handles), _f32(canonical), _f32(R)
+    N, V, _ = s.shape
+    out = np.zeros(s.shape, np.float64)
+    lib().or_skinning(N, V, _p(s, f32p), _p(a, f32p), _p(h, f32p), _p(c, f32p), _p(r, f32p),
+                      _p(out, f64p), float(beta))
+    return out
+
+
+def sort_frags(pix, attrs):
+    """Canonical order (batch, prim id, h, w) used by the golden fixtures."""
+    if pix.shape[0] == 0:
+        return pix, attrs
+    key = np.lexsort((pix[:, 2], pix[:, 1], attrs[:, 3], pix[:, 0]))
+    return pix[key], attrs[key]
