@@ -1,0 +1,137 @@
+/*
+ * s2c.h -- C ABI of the GB300 strands-to-cards raster path (libs2c.so).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream, launches
+ * sm_103a kernels on that stream and returns an s2c_status (never exits the process).
+ * Outputs and scratch ("workspace") are allocated by the caller; each entry that needs
+ * scratch has a *_workspace_size() query.  Entries that return a count to the host
+ * (the reference's drop-in surface does) synchronise the stream; all others are
+ * asynchronous.
+ *
+ * The "replaces" line of each entry names the reference interface it stands in for,
+ * as a path inside the reference project (pystrns2cards/src/pystrns2cards.cpp is the
+ * nanobind module `_core`; the launchers live in the *.cu files next to it).
+ *
+ * Layouts (all C-contiguous, little-endian):
+ *   pos     float32 (B, V, 4)   homogeneous clip-space vertex positions, one set per view
+ *   edges   int32   (E, 2)      vertex indices of line segments / mesh edges
+ *   tri     int32   (T, 3)
+ *   bitset  int32   (B, H, W, S), S = ceil(K / 32); cluster c is bit c % 32 of slot c / 32
+ *   frag_pix int32 (F, 3) = (view, row, col); frag_attrs float32 (F, 4)
+ */
+#ifndef S2C_H
+#define S2C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define S2C_API __attribute__((visibility("default")))
+#else
+#define S2C_API
+#endif
+
+typedef int s2c_status;
+#define S2C_OK 0
+#define S2C_ERR_INVALID 1     /* bad shape, size, pointer or argument               */
+#define S2C_ERR_CUDA 2        /* a CUDA runtime call or kernel launch failed         */
+#define S2C_ERR_WORKSPACE 3   /* caller workspace smaller than *_workspace_size()    */
+#define S2C_ERR_TIMEOUT 4     /* a bounded device-side wait gave up                  */
+
+/* a cudaStream_t; NULL = the legacy default stream */
+typedef struct CUstream_st* s2c_stream;
+
+S2C_API int s2c_version(void);
+/* message of the last failed call on this host thread ("" if none) */
+S2C_API const char* s2c_last_error(void);
+
+/* ---------------------------------------------------------------------------------- *
+ * DDA line raster                                                                     *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: dda_compute_span (pystrns2cards.cpp:531-565; dda.cu:89-122).
+ * Per primitive p (edge id edge_ids[p] = b*E + e, or p itself when edge_ids is NULL):
+ * fragment count, (axis, slope) and (start_x, start_y, offset0, offset1); writes the
+ * inclusive int32 prefix sum of the counts.  When num_frags != NULL the total is copied
+ * to the host (stream synchronised), as the reference's return value. */
+S2C_API size_t s2c_dda_compute_span_workspace_size(int64_t num_prims);
+S2C_API s2c_status s2c_dda_compute_span(int64_t num_prims, const int32_t* edge_ids, int H, int W,
+                                int B, int V, const float* pos, int E, const int32_t* edges,
+                                int32_t* frag_prefix_sum, float* frag_slopes, float* frag_spans,
+                                void* workspace, size_t workspace_bytes, int64_t* num_frags,
+                                s2c_stream stream);
+
+/* replaces: dda_compute_fragments (pystrns2cards.cpp:567-611; dda.cu:146-256).
+ * frag_pix must be pre-filled with -1 (rejected fragments keep -1, as in the reference). */
+S2C_API s2c_status s2c_dda_compute_fragments(int64_t num_prims, int64_t num_frags,
+                                     const int32_t* frag_prefix_sum, const int32_t* edge_ids,
+                                     const float* frag_slopes, const float* frag_spans, int H,
+                                     int W, int B, int V, const float* pos, int E,
+                                     const int32_t* edges, int32_t* frag_pix,
+                                     float* frag_attrs, s2c_stream stream);
+
+/* replaces: filter_valid_fragments (pystrns2cards.cpp:358-392; rasterize.cu:280-365).
+ * Keeps fragments with frag_pix[i,0] >= 0 in their original order (the reference's order
+ * depends on block scheduling); the kept count goes to *num_valid (host, synchronising). */
+S2C_API size_t s2c_filter_valid_fragments_workspace_size(int64_t num_frags);
+S2C_API s2c_status s2c_filter_valid_fragments(int64_t num_frags, const int32_t* frag_pix,
+                                      const float* frag_attrs, int32_t* frag_pix_out,
+                                      float* frag_attrs_out, void* workspace,
+                                      size_t workspace_bytes, int64_t* num_valid,
+                                      s2c_stream stream);
+
+/* replaces: cluster_mask_from_fragments (pystrns2cards.cpp:440-478; rasterize.cu:474-520).
+ * ORs bit prim2cluster[prim] of every fragment into a caller-zeroed bitset (B, H, W, S). */
+S2C_API s2c_status s2c_cluster_mask_from_fragments(int64_t num_frags, const int32_t* frag_pix,
+                                           const float* frag_attrs, const int32_t* prim2cluster,
+                                           int64_t num_prims, int B, int H, int W, int S,
+                                           int32_t* bitset, s2c_stream stream);
+
+/* new (no single reference call; = dda_compute_fragments followed by
+ * cluster_mask_from_fragments, as 3_fitting.py:254-261 uses them).
+ * Rasterises every primitive straight into the bitset without a fragment list: segments
+ * are binned into screen tiles, each tile's bitset is assembled in shared memory and
+ * written once with coalesced stores.  The whole bitset (B, H, W, S) is overwritten.
+ * edge_ids may be NULL (all B*E segments).  Bit-identical to the reference composition. */
+S2C_API size_t s2c_dda_cluster_bitset_workspace_size(int64_t num_prims, int B, int H, int W, int S);
+S2C_API s2c_status s2c_dda_cluster_bitset(int64_t num_prims, const int32_t* edge_ids, int H, int W,
+                                  int B, int V, const float* pos, int E, const int32_t* edges,
+                                  const int32_t* prim2cluster, int S, int32_t* bitset,
+                                  void* workspace, size_t workspace_bytes, s2c_stream stream);
+/* after a call on the same stream (synchronise first): how many primitives took the
+ * global-atomic fallback because the workspace or a tile's record list was full */
+S2C_API s2c_status s2c_dda_cluster_bitset_stats(const void* workspace, size_t workspace_bytes,
+                                        int64_t* entries, int64_t* overflow_prims);
+
+/* ---------------------------------------------------------------------------------- *
+ * stream compaction                                                                   *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: compact_valid_ints (pystrns2cards.cpp:774-786; compact_utils.cu:54-77).
+ * Order-preserving; count to *num_valid (host, synchronising). */
+S2C_API size_t s2c_compact_valid_ints_workspace_size(int64_t n);
+S2C_API s2c_status s2c_compact_valid_ints(int64_t n, const int32_t* input, int32_t* output,
+                                  void* workspace, size_t workspace_bytes, int64_t* num_valid,
+                                  s2c_stream stream);
+
+/* ---------------------------------------------------------------------------------- *
+ * bitset utilities                                                                    *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: popcount_bitset (pystrns2cards.cpp:507-529; bitset_utils.cu:37-52,392-404) */
+S2C_API s2c_status s2c_popcount_bitset(int64_t num_pixels, int S, const int32_t* bitset,
+                               float* count_image, s2c_stream stream);
+
+/* replaces: accumulate_bitset_rgb (pystrns2cards.cpp:480-505; bitset_utils.cu:6-35,376-390) */
+S2C_API s2c_status s2c_accumulate_bitset_rgb(int64_t num_pixels, int S, const int32_t* bitset,
+                                     int num_clusters, const float* cluster_rgb,
+                                     float* accum_color, s2c_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* S2C_H */

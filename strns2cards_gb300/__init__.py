@@ -1,1 +1,10 @@
-"""GB300-native strands-to-cards rasterization path (sm_103a CUDA behind a C ABI)."""
+"""GB300-native strands-to-cards raster path: sm_103a CUDA kernels behind a C ABI.
+
+The public ops keep the names and contracts of the reference package ``pystrns2cards``
+so that ``import strns2cards_gb300 as s2c`` replaces ``import pystrns2cards as s2c``.
+"""
+from .bitset_utils import accumulate_bitset_rgb, popcount_bitset  # noqa: F401
+from .dda import dda_cluster_bitset, dda_compute_fragments  # noqa: F401
+from .mesh import build_edges_from_triangles  # noqa: F401
+from .rasterize import cluster_mask_from_fragments  # noqa: F401
+from . import _core  # noqa: F401

@@ -1,0 +1,198 @@
+"""Drop-in for the reference's compiled ``pystrns2cards._core`` module.
+
+Each function keeps the name, argument order, dtype/shape contract and return value of
+the corresponding ``m.def`` in ``pystrns2cards/src/pystrns2cards.cpp`` and forwards to
+the C ABI of libs2c.so (include/s2c.h) on the tensor's current CUDA stream.  Argument
+type errors raise TypeError (as nanobind does), validation failures RuntimeError, like
+the reference's ``std::runtime_error``.  Temporaries come from the torch caching
+allocator as workspace; the C side never allocates.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import call, ptr, workspace
+
+_f32, _i32 = torch.float32, torch.int32
+
+
+def _arr(t, dtype, ndim=None, last=None, name="array"):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name}: expected a torch.Tensor, got {type(t).__name__}")
+    if t.dtype != dtype:
+        raise TypeError(f"{name}: expected dtype {dtype}, got {t.dtype}")
+    if ndim is not None and t.ndim != ndim:
+        raise TypeError(f"{name}: expected {ndim} dimensions, got {t.ndim}")
+    if last is not None and t.shape[-1] != last:
+        raise TypeError(f"{name}: expected last dimension {last}, got {t.shape[-1]}")
+    if not t.is_contiguous():
+        raise TypeError(f"{name}: expected a C-contiguous tensor")
+    return t
+
+
+def _cuda(*ts, msg="All tensors must be CUDA tensors."):
+    for t in ts:
+        if t is not None and not t.is_cuda:
+            raise RuntimeError(msg)
+
+
+def _stream(t):
+    return _lib.stream_of(t)
+
+
+def print_version():
+    print(f"strns2cards_gb300 C ABI version {_lib.lib().s2c_version()}")
+
+
+# ---- DDA (pystrns2cards.cpp:531-611) -------------------------------------------------
+def dda_compute_span(edge_ids, H, W, pos, edges, frag_prefix_sum, frag_slopes, frag_spans) -> int:
+    _arr(edge_ids, _i32, 1, name="edge_ids")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _arr(frag_slopes, _f32, 2, 2, "frag_slopes")
+    _arr(frag_spans, _f32, 2, 4, "frag_spans")
+    _cuda(edge_ids, pos, edges, frag_prefix_sum, frag_slopes, frag_spans)
+    P = edge_ids.shape[0]
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    if frag_prefix_sum.shape[0] != P or frag_slopes.shape[0] != P or frag_spans.shape[0] != P:
+        raise RuntimeError("Invalid output tensor shapes for frag_prefix_sum, frag_slopes, or frag_spans.")
+    L = _lib.lib()
+    ws = workspace(L.s2c_dda_compute_span_workspace_size(P), pos.device)
+    n = _lib.i64_out()
+    call("s2c_dda_compute_span", P, ptr(edge_ids), int(H), int(W), B, V, ptr(pos), E, ptr(edges),
+         ptr(frag_prefix_sum), ptr(frag_slopes), ptr(frag_spans), ptr(ws), ws.numel(), ctypes.byref(n),
+         _stream(pos))
+    return int(n.value)
+
+
+def dda_compute_fragments(frag_prefix_sum, edge_ids, frag_slopes, frag_spans, H, W, pos, edges, frag_pix,
+                          frag_attrs) -> None:
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _arr(edge_ids, _i32, 1, name="edge_ids")
+    _arr(frag_slopes, _f32, 2, 2, "frag_slopes")
+    _arr(frag_spans, _f32, 2, 4, "frag_spans")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(frag_pix, _i32, 2, 3, "frag_pix")
+    _arr(frag_attrs, _f32, 2, 4, "frag_attrs")
+    _cuda(frag_prefix_sum, edge_ids, frag_slopes, frag_spans, pos, edges, frag_pix, frag_attrs)
+    F = frag_pix.shape[0]
+    P = edge_ids.shape[0]
+    if (frag_prefix_sum.shape[0] != P or frag_slopes.shape[0] != P or frag_spans.shape[0] != P
+            or frag_attrs.shape[0] != F):
+        raise RuntimeError("Invalid shape for input or output arrays.")
+    B, V, _ = pos.shape
+    call("s2c_dda_compute_fragments", P, F, ptr(frag_prefix_sum), ptr(edge_ids), ptr(frag_slopes), ptr(frag_spans),
+         int(H), int(W), B, V, ptr(pos), edges.shape[0], ptr(edges), ptr(frag_pix), ptr(frag_attrs), _stream(pos))
+
+
+# ---- fragments (pystrns2cards.cpp:358-392, 440-478) ----------------------------------
+def filter_valid_fragments(frag_pix, frag_attrs, frag_pix_out, frag_attrs_out) -> int:
+    for t, d, last, nm in ((frag_pix, _i32, 3, "frag_pix"), (frag_attrs, _f32, 4, "frag_attrs"),
+                           (frag_pix_out, _i32, 3, "frag_pix_out"), (frag_attrs_out, _f32, 4, "frag_attrs_out")):
+        _arr(t, d, 2, last, nm)
+    _cuda(frag_pix, frag_attrs, frag_pix_out, frag_attrs_out, msg="All tensors must be CUDA tensors (device_id >= 0).")
+    F = frag_pix.shape[0]
+    if frag_attrs.shape[0] != F or frag_pix_out.shape[0] != F or frag_attrs_out.shape[0] != F:
+        raise RuntimeError("Mismatch in fragment counts between input/output tensors.")
+    if F == 0:
+        return 0
+    L = _lib.lib()
+    ws = workspace(L.s2c_filter_valid_fragments_workspace_size(F), frag_pix.device)
+    n = _lib.i64_out()
+    call("s2c_filter_valid_fragments", F, ptr(frag_pix), ptr(frag_attrs), ptr(frag_pix_out), ptr(frag_attrs_out),
+         ptr(ws), ws.numel(), ctypes.byref(n), _stream(frag_pix))
+    return int(n.value)
+
+
+def cluster_mask_from_fragments(frag_pix, frag_attrs, prim2cluster, bitset) -> None:
+    _arr(frag_pix, _i32, 2, 3, "frag_pix")
+    _arr(frag_attrs, _f32, 2, 4, "frag_attrs")
+    _arr(prim2cluster, _i32, 1, name="prim2cluster")
+    _arr(bitset, _i32, 4, name="bitset")
+    _cuda(frag_pix, frag_attrs, prim2cluster, bitset, msg="All tensors must be CUDA tensors (device_id >= 0).")
+    F = frag_pix.shape[0]
+    if frag_attrs.shape[0] != F:
+        raise RuntimeError("frag_pix and frag_attrs must have the same number of fragments.")
+    B, H, W, S = bitset.shape
+    call("s2c_cluster_mask_from_fragments", F, ptr(frag_pix), ptr(frag_attrs), ptr(prim2cluster),
+         prim2cluster.shape[0], B, H, W, S, ptr(bitset), _stream(bitset))
+
+
+# ---- bitsets (pystrns2cards.cpp:480-529) ---------------------------------------------
+def accumulate_bitset_rgb(bitset, cluster_rgb, accum_color) -> None:
+    _arr(bitset, _i32, 4, name="bitset")
+    _arr(cluster_rgb, _f32, 2, 3, "cluster_rgb")
+    _arr(accum_color, _f32, 4, 3, "accum_color")
+    _cuda(bitset, cluster_rgb, accum_color, msg="All tensors must be on CUDA")
+    B, H, W, S = bitset.shape
+    K = cluster_rgb.shape[0]
+    if S * 32 < K:
+        raise RuntimeError("Too few slots for the number of clusters.")
+    call("s2c_accumulate_bitset_rgb", B * H * W, S, ptr(bitset), K, ptr(cluster_rgb), ptr(accum_color),
+         _stream(bitset))
+
+
+def popcount_bitset(bitset, count_image) -> None:
+    _arr(bitset, _i32, 4, name="bitset")
+    _arr(count_image, _f32, 3, name="count_image")
+    _cuda(bitset, count_image, msg="All tensors must be on CUDA")
+    B, H, W, S = bitset.shape
+    if tuple(count_image.shape) != (B, H, W):
+        raise RuntimeError("count_image must have shape [B, H, W]")
+    call("s2c_popcount_bitset", B * H * W, S, ptr(bitset), ptr(count_image), _stream(bitset))
+
+
+# ---- compaction (pystrns2cards.cpp:774-786) ------------------------------------------
+def compact_valid_ints(input, output) -> int:
+    _arr(input, _i32, 1, name="input")
+    _arr(output, _i32, 1, name="output")
+    _cuda(input, output, msg="compact_valid_ints: both input and output must be CUDA tensors.")
+    if input.shape[0] != output.shape[0]:
+        raise RuntimeError("compact_valid_ints: input and output must have the same size.")
+    N = input.shape[0]
+    if N == 0:
+        return 0
+    L = _lib.lib()
+    ws = workspace(L.s2c_compact_valid_ints_workspace_size(N), input.device)
+    n = _lib.i64_out()
+    call("s2c_compact_valid_ints", N, ptr(input), ptr(output), ptr(ws), ws.numel(), ctypes.byref(n), _stream(input))
+    return int(n.value)
+
+
+# ---- fused entries (no reference counterpart) ----------------------------------------
+def dda_cluster_bitset(pos, edges, prim2cluster, bitset, edge_ids=None, ws=None) -> torch.Tensor:
+    """Fused DDA -> cluster bitset into ``bitset`` (B, H, W, S), fully overwritten."""
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(prim2cluster, _i32, 1, name="prim2cluster")
+    _arr(bitset, _i32, 4, name="bitset")
+    if edge_ids is not None:
+        _arr(edge_ids, _i32, 1, name="edge_ids")
+    _cuda(pos, edges, prim2cluster, bitset, edge_ids)
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    if prim2cluster.shape[0] < E:
+        raise RuntimeError("prim2cluster must have one entry per edge.")
+    if bitset.shape[0] != B:
+        raise RuntimeError("bitset must have one image per view of pos.")
+    _, H, W, S = bitset.shape
+    P = B * E if edge_ids is None else edge_ids.shape[0]
+    L = _lib.lib()
+    need = L.s2c_dda_cluster_bitset_workspace_size(P, B, H, W, S)
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, pos.device)
+    call("s2c_dda_cluster_bitset", P, ptr(edge_ids), H, W, B, V, ptr(pos), E, ptr(edges), ptr(prim2cluster), S,
+         ptr(bitset), ptr(ws), ws.numel(), _stream(pos))
+    return bitset
+
+
+def dda_cluster_bitset_stats(ws) -> tuple:
+    e, o = _lib.i64_out(), _lib.i64_out()
+    call("s2c_dda_cluster_bitset_stats", ptr(ws), ws.numel(), ctypes.byref(e), ctypes.byref(o))
+    return int(e.value), int(o.value)

@@ -1,0 +1,651 @@
+// Fused DDA line raster -> per-pixel cluster bitset (s2c_dda_cluster_bitset).
+//
+// Same bits as the reference's dda_compute_fragments followed by
+// cluster_mask_from_fragments (dda.cu:9-256, rasterize.cu:474-520), without a fragment
+// list and without global atomics in the common case.  Launches, all on one stream:
+//
+//  init     zero the per-call counters.
+//  bin      one CTA per chunk of 2048 primitives.  Each warp walks 32 segments in
+//           lockstep, one fragment per step, with the reference's exact FP32 arithmetic
+//           (bounds and depth tests included; the depth test is skipped where both end
+//           points are provably inside the clip volume).  Accepted fragments are encoded
+//           as runs: one 8-byte entry holds the cluster, the first pixel inside a screen
+//           tile and one bit per further step along the minor axis, so a run needs no
+//           floating point to replay.  Entries are grouped by tile in shared memory
+//           (hash of tile ids, warp-aggregated counters), written contiguously per tile,
+//           and one (tile, start, count) record per touched tile goes to a record pool.
+//  scan     exclusive offsets of the per-tile record counts.
+//  scatter  records sorted by tile; tiles with many entries listed first.
+//  raster   persistent CTAs take tiles from a queue (heavy ones first): clear a
+//           shared-memory copy of the tile's bitset, replay its entries with
+//           shared-memory atomicOr, write the whole tile (zeros included) once with
+//           coalesced 16-byte streaming stores.
+//  fixup    chunks whose entries did not fit (chunk buffer, hash table, entry or record
+//           pool) are rasterised with global atomicOr on top of the finished bitset.
+#include <algorithm>
+
+#include "lines.cuh"
+#include "scan.cuh"
+
+namespace s2c {
+
+constexpr int kBinThreads = 256;
+constexpr int kBinPPT = 8;
+constexpr int kChunk = kBinThreads * kBinPPT;  // primitives per bin CTA
+constexpr int kHT = 1024;                      // tile hash slots per chunk
+constexpr int kStage = 16;                     // staged entries per bin thread
+constexpr int kSpill = 1024;                   // shared spill entries per chunk
+constexpr int kRasterThreads = 512;
+constexpr int kMaxRun = 28;                    // fragments per entry (27 step bits)
+constexpr int kHeavy = 8192;                   // entries that make a tile "heavy"
+
+enum { H_ENT = 0, H_REC = 1, H_OVER = 2, H_BAD = 3, H_WORK = 4, H_HEAVY = 5, H_WORDS = 16 };
+
+struct Geo {
+    int B, H, W, S;
+    int twl, thl;  // log2 tile width / height
+    int tiles_x, tiles_y;
+    int num_tiles;
+};
+
+struct Ws {
+    long long* hdr;
+    int32_t* nrec;      // records per tile
+    int32_t* nent;      // entries per tile
+    int32_t* rfill;     // scatter cursors
+    int32_t* roff;      // exclusive record offsets (inclusive scan, then shifted on use)
+    int32_t* heavy;     // heavy tile list
+    int32_t* over;      // overflowed chunk ids
+    int4* recs;         // (tile, start, count, -)
+    int2* sorted;       // (start, count) grouped by tile
+    uint2* entries;
+    void* scan_ws;      // scan scratch
+    int64_t scan_total_off;
+    int64_t entry_cap, rec_cap, chunk_cap;
+};
+
+static Geo make_geo(int B, int H, int W, int S) {
+    Geo g;
+    g.B = B; g.H = H; g.W = W; g.S = S;
+    // <= 64 KiB of bitset per tile, >= 64 px, and enough tiles to spread over the GPU
+    const int64_t cap_px = std::max<int64_t>(64, std::min<int64_t>(4096, 16384 / std::max(S, 1)));
+    const int64_t want = 4LL * num_sms();
+    int lg = 6;
+    while ((1LL << (lg + 1)) <= cap_px && ((int64_t)B * H * W) >> (lg + 1) >= want) ++lg;
+    g.twl = (lg + 1) / 2;
+    g.thl = lg / 2;
+    g.tiles_x = (W + (1 << g.twl) - 1) >> g.twl;
+    g.tiles_y = (H + (1 << g.thl) - 1) >> g.thl;
+    g.num_tiles = (int)((int64_t)B * g.tiles_x * g.tiles_y);
+    return g;
+}
+
+// Workspace layout; with base == nullptr only the sizes are computed.
+static size_t layout(void* base, size_t bytes, int64_t P, const Geo& g, Ws& w) {
+    Carver c(base, bytes);
+    const int64_t T = g.num_tiles;
+    w.hdr = c.take<long long>(H_WORDS);
+    w.nrec = c.take<int32_t>(T);
+    w.nent = c.take<int32_t>(T);
+    w.rfill = c.take<int32_t>(T);
+    w.roff = c.take<int32_t>(T);
+    w.heavy = c.take<int32_t>(T);
+    w.chunk_cap = std::max<int64_t>((P + kChunk - 1) / kChunk, 1);
+    w.over = c.take<int32_t>(w.chunk_cap);
+    w.rec_cap = std::max<int64_t>(P / 4, 1 << 16);
+    w.recs = c.take<int4>(w.rec_cap);
+    w.sorted = c.take<int2>(w.rec_cap);
+    w.scan_ws = c.take<char>(scan_workspace_bytes(T) + 256);
+    w.scan_total_off = (int64_t)scan_workspace_bytes(T);
+    const size_t fixed = align_up(c.off, 256);
+    w.entries = (uint2*)(c.base + fixed);
+    w.entry_cap = bytes > fixed ? std::min<int64_t>((int64_t)((bytes - fixed) / sizeof(uint2)), 0x7fffffffLL) : 0;
+    return fixed;
+}
+
+__global__ void fused_init(long long* hdr, int32_t* nrec, int32_t* nent, int32_t* rfill, int T) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < H_WORDS) hdr[i] = 0;
+    for (int t = i; t < T; t += gridDim.x * blockDim.x) {
+        nrec[t] = 0;
+        nent[t] = 0;
+        rfill[t] = 0;
+    }
+}
+
+__device__ __forceinline__ int ht_slot(int* keys, int key) {
+    unsigned h = ((unsigned)key * 2654435761u) >> 22;  // 10 bits
+    for (int probe = 0; probe < kHT; ++probe) {
+        const int k = ((volatile int*)keys)[h];
+        if (k == key) return (int)h;
+        if (k == -1) {
+            const int old = atomicCAS(keys + h, -1, key);
+            if (old == -1 || old == key) return (int)h;
+        }
+        h = (h + 1) & (kHT - 1);
+    }
+    return -1;
+}
+
+// cluster of edge e; the reference carries the prim id as float(e + 1)
+__device__ __forceinline__ int cluster_of(const int32_t* __restrict__ p2c, int e, int E, int S, long long* bad) {
+    const int pr = prim_roundtrip(e);
+    if (pr < 0 || pr >= E) {
+        atomicAdd((unsigned long long*)bad, 1ull);
+        return -1;
+    }
+    const int c = __ldg(p2c + pr);
+    if (c < 0 || c >= 32 * S) {
+        atomicAdd((unsigned long long*)bad, 1ull);
+        return -1;
+    }
+    return c;
+}
+
+// Depth test skipped when both ends are finite, 1e-30 <= w <= 1e30 and |z| <= 0.999 w:
+// then for every t1 in [0, 1] the reference's z = (t0 z0 + t1 z1) / (t0 w0 + t1 w1),
+// rounded, has |z| <= 0.999 (1 + 5 eps) < 1, so every fragment passes.
+__device__ __forceinline__ bool depth_always_passes(float4 a, float4 b) {
+    auto ok = [](float4 p) {
+        return isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w >= 1e-30f && p.w <= 1e30f &&
+               fabsf(p.z) <= 0.999f * p.w;
+    };
+    return ok(a) && ok(b);
+}
+
+struct Lane {
+    bool valid;
+    Prim q;
+};
+
+__device__ __forceinline__ Lane fetch(int64_t p, int64_t P, const Lines& L) {
+    Lane l;
+    l.valid = p < P && load_prim(p, L, l.q);
+    return l;
+}
+
+__global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L, Geo g, const int32_t* __restrict__ p2c,
+                                                              Ws w) {
+    extern __shared__ int smem[];
+    int* ht_key = smem;
+    int* ht_cnt = ht_key + kHT;
+    int* ht_base = ht_cnt + kHT;
+    // lane-private staging, entry i of thread t at [i * kBinThreads + t] (conflict-free)
+    uint2* st_pay = (uint2*)(ht_base + kHT);                              // kStage * kBinThreads
+    uint32_t* st_key = (uint32_t*)(st_pay + kStage * kBinThreads);        // slot | tick << 10
+    uint2* sp_pay = (uint2*)(st_key + kStage * kBinThreads);              // shared spill area
+    uint32_t* sp_key = (uint32_t*)(sp_pay + kSpill);
+    __shared__ int s_spill, s_over, s_nslots, s_reserved, s_total;
+    __shared__ long long s_base, s_rbase;
+    __shared__ int wb[32];
+
+    for (int i = threadIdx.x; i < kHT; i += blockDim.x) {
+        ht_key[i] = -1;
+        ht_cnt[i] = 0;
+    }
+    if (threadIdx.x == 0) {
+        s_spill = 0;
+        s_over = 0;
+        s_reserved = 0;
+    }
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31;
+    const int64_t chunk0 = (int64_t)blockIdx.x * kChunk;
+    const int TW = 1 << g.twl, TH = 1 << g.thl;
+    int n_st = 0;                  // staged entries of this thread
+    int last_tile = -1, last_slot = -1;
+    auto emit = [&](int tile, uint2 pay) {
+        int slot = last_slot;
+        if (tile != last_tile) {
+            slot = ht_slot(ht_key, tile);
+            if (slot < 0) { s_over = 1; return; }
+            last_tile = tile;
+            last_slot = slot;
+        }
+        const int tick = atomicAdd(ht_cnt + slot, 1);
+        const uint32_t key = (uint32_t)slot | ((uint32_t)tick << 10);
+        if (n_st < kStage) {
+            st_pay[n_st * kBinThreads + threadIdx.x] = pay;
+            st_key[n_st * kBinThreads + threadIdx.x] = key;
+            ++n_st;
+        } else {
+            const int i = atomicAdd(&s_spill, 1);
+            if (i < kSpill) {
+                sp_pay[i] = pay;
+                sp_key[i] = key;
+            } else {
+                s_over = 1;
+            }
+        }
+    };
+
+    Lane cur = fetch(chunk0 + threadIdx.x, P, L);
+    for (int j = 0; j < kBinPPT; ++j) {
+        Lane nxt;  // prefetch the next primitive of this thread
+        nxt.valid = false;
+        if (j + 1 < kBinPPT) nxt = fetch(chunk0 + (int64_t)(j + 1) * kBinThreads + threadIdx.x, P, L);
+        if (cur.valid) {
+            const Span s = dda_span(cur.q.p0, cur.q.p1, g.H, g.W);
+            const int c = s.count > 0 ? cluster_of(p2c, cur.q.e, L.E, g.S, w.hdr + H_BAD) : -1;
+            if (c >= 0) {
+                const bool zfast = depth_always_passes(cur.q.p0, cur.q.p1);
+                const int axis = s.axis != 0.f;
+                const uint32_t xbase = (uint32_t)c | ((uint32_t)axis << 28);
+                const int tbase = cur.q.b * g.tiles_y;
+                // major / minor view of the sweep
+                const float smaj = axis ? s.sy : s.sx, smin = axis ? s.sx : s.sy;
+                const int nmaj = axis ? g.H : g.W, nmin = axis ? g.W : g.H;
+                const int lgmaj = axis ? g.thl : g.twl, lgmin = axis ? g.twl : g.thl;
+                const int last = s.count - 1;
+                auto sample = [&](int k, int& im, int& in) {
+                    const float d = fminf(fmaxf(__fadd_rn((float)k, 0.5f), s.off0), s.off1);
+                    im = f2i(floorf(__fadd_rn(smaj, d)));
+                    in = f2i(floorf(__fadd_rn(smin, __fmul_rn(d, s.slope))));
+                };
+                int m0, n0, ml, nl;
+                sample(0, m0, n0);
+                sample(last, ml, nl);
+                // Simple sweep: every fragment passes the depth test, both end fragments are
+                // inside the image (coordinates are monotonic in k, so all are), and the
+                // major pixel is start + k (exact for interior samples d = k + 0.5; checked
+                // at both ends).  Then only the minor coordinate needs evaluating.
+                const bool simple = zfast && isfinite(s.slope) && m0 == f2i(smaj) && ml == m0 + last &&
+                                    m0 >= 0 && ml < nmaj && min(n0, nl) >= 0 && max(n0, nl) < nmin;
+                if (simple) {
+                    const int dir = s.slope >= 0.f ? 1 : -1;
+                    const uint32_t dbit = (uint32_t)(dir < 0) << 29;
+                    const int TM = 1 << lgmaj;
+                    int kcross = TM - (m0 & (TM - 1));
+                    auto start = [&](int im, int in, int& tile, int& lp) {
+                        const int h = axis ? im : in, wv = axis ? in : im;
+                        tile = (tbase + (h >> g.thl)) * g.tiles_x + (wv >> g.twl);
+                        lp = (h & (TH - 1)) * TW + (wv & (TW - 1));
+                    };
+                    int r_tile, r_lp;
+                    start(m0, n0, r_tile, r_lp);
+                    int r_n = 1, prev = n0;
+                    unsigned r_steps = 0;
+                    for (int k = 1; k <= last; ++k) {
+                        const float d = fminf(fmaxf(__fadd_rn((float)k, 0.5f), s.off0), s.off1);
+                        const int in = f2i(floorf(__fadd_rn(smin, __fmul_rn(d, s.slope))));
+                        const int dm = in - prev;
+                        if (k == kcross || ((in ^ prev) >> lgmin) != 0 || r_n == kMaxRun || (dm != 0 && dm != dir)) {
+                            emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | dbit,
+                                                    (uint32_t)(r_n - 1) | (r_steps << 5)));
+                            start(m0 + k, in, r_tile, r_lp);
+                            r_n = 1;
+                            r_steps = 0;
+                            if (k == kcross) kcross += TM;
+                        } else {
+                            r_steps |= (uint32_t)(dm != 0) << (r_n - 1);
+                            ++r_n;
+                        }
+                        prev = in;
+                    }
+                    emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | dbit, (uint32_t)(r_n - 1) | (r_steps << 5)));
+                } else {
+                    // general sweep: every fragment tested as in the reference
+                    int r_n = 0, r_tile = -1, r_lp = 0, r_dir = 0, r_lh = 0, r_lw = 0;
+                    unsigned r_steps = 0;
+                    for (int k = 0; k < s.count; ++k) {
+                        float x, y;
+                        dda_sample(s, k, x, y);
+                        const int h = f2i(floorf(y)), wv = f2i(floorf(x));
+                        bool acc = h >= 0 && h < g.H && wv >= 0 && wv < g.W;
+                        if (acc && !zfast) {
+                            const float t1 = dda_t1(cur.q.p0, cur.q.p1, x, y, s.axis, g.H, g.W);
+                            acc = z_ok(dda_z(cur.q.p0, cur.q.p1, t1));
+                        }
+                        int tile = -1, lh = 0, lw = 0, dmin = 0;
+                        bool extend = false;
+                        if (acc) {
+                            tile = (tbase + (h >> g.thl)) * g.tiles_x + (wv >> g.twl);
+                            lh = h & (TH - 1);
+                            lw = wv & (TW - 1);
+                            if (r_n > 0 && tile == r_tile && r_n < kMaxRun) {
+                                const int dmaj = axis ? lh - r_lh : lw - r_lw;
+                                dmin = axis ? lw - r_lw : lh - r_lh;
+                                extend = dmaj == 1 &&
+                                         (dmin == 0 || ((dmin == 1 || dmin == -1) && (r_dir == 0 || dmin == r_dir)));
+                            }
+                        }
+                        if (extend) {
+                            if (dmin) {
+                                r_steps |= 1u << (r_n - 1);
+                                r_dir = dmin;
+                            }
+                            ++r_n;
+                            r_lh = lh;
+                            r_lw = lw;
+                            continue;
+                        }
+                        if (r_n > 0)
+                            emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | ((uint32_t)(r_dir < 0) << 29),
+                                                    (uint32_t)(r_n - 1) | (r_steps << 5)));
+                        r_n = 0;
+                        if (acc) {
+                            r_n = 1;
+                            r_tile = tile;
+                            r_lp = lh * TW + lw;
+                            r_dir = 0;
+                            r_steps = 0;
+                            r_lh = lh;
+                            r_lw = lw;
+                        }
+                    }
+                    if (r_n > 0)
+                        emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | ((uint32_t)(r_dir < 0) << 29),
+                                                (uint32_t)(r_n - 1) | (r_steps << 5)));
+                }
+            }
+        }
+        cur = nxt;
+    }
+    __syncthreads();
+    // exclusive scans over the slots: entry offsets and record ranks (4 slots per thread)
+    int v[4], used[4], sv = 0, su = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        v[j] = ht_cnt[threadIdx.x * 4 + j];
+        used[j] = v[j] > 0;
+        sv += v[j];
+        su += used[j];
+    }
+    const int packed = min(sv, 0xffff) | (su << 16);
+    int inc = packed;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    const int warp = threadIdx.x >> 5;
+    if (lane == 31) wb[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        const int x = lane < (kBinThreads >> 5) ? wb[lane] : 0;
+        int xi = x;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, xi, o);
+            if (lane >= o) xi += t;
+        }
+        if (lane < (kBinThreads >> 5)) wb[lane] = xi - x;
+        if (lane == (kBinThreads >> 5) - 1) {
+            s_nslots = xi >> 16;
+            s_total = xi & 0xffff;
+        }
+    }
+    __syncthreads();
+    int run = wb[warp] + inc - packed;
+    int ebase[4], rrank[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        ebase[j] = run & 0xffff;
+        rrank[j] = run >> 16;
+        ht_base[threadIdx.x * 4 + j] = ebase[j];
+        run += v[j] | (used[j] << 16);
+    }
+    if (threadIdx.x == 0 && !s_over) {
+        const long long b = atomicAdd((unsigned long long*)(w.hdr + H_ENT), (unsigned long long)s_total);
+        const long long r = atomicAdd((unsigned long long*)(w.hdr + H_REC), (unsigned long long)s_nslots);
+        s_base = b;
+        s_rbase = r;
+        s_reserved = 1;
+        if (b + s_total > w.entry_cap || r + s_nslots > w.rec_cap) s_over = 1;
+    }
+    __syncthreads();
+    if (s_over) {
+        // record slots reserved by this chunk stay in the pool: mark them empty
+        if (s_reserved)
+            for (long long r = s_rbase + threadIdx.x; r < min(s_rbase + s_nslots, (long long)w.rec_cap); r += blockDim.x)
+                w.recs[r] = make_int4(-1, 0, 0, 0);
+        if (threadIdx.x == 0) {
+            const long long o = atomicAdd((unsigned long long*)(w.hdr + H_OVER), 1ull);
+            if (o < w.chunk_cap) w.over[o] = (int32_t)blockIdx.x;
+        }
+        return;
+    }
+    const long long base = s_base;
+    for (int i = 0; i < n_st; ++i) {
+        const uint32_t key = st_key[i * kBinThreads + threadIdx.x];
+        w.entries[base + ht_base[key & 1023] + (key >> 10)] = st_pay[i * kBinThreads + threadIdx.x];
+    }
+    const int nsp = min(s_spill, kSpill);
+    for (int i = threadIdx.x; i < nsp; i += blockDim.x) {
+        const uint32_t key = sp_key[i];
+        w.entries[base + ht_base[key & 1023] + (key >> 10)] = sp_pay[i];
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        if (!used[j]) continue;
+        const int tile = ht_key[threadIdx.x * 4 + j];
+        w.recs[s_rbase + rrank[j]] = make_int4(tile, (int)(base + ebase[j]), v[j], 0);
+        atomicAdd(w.nrec + tile, 1);
+        atomicAdd(w.nent + tile, v[j]);
+    }
+}
+
+// records -> grouped by tile (roff holds the inclusive scan of nrec); heavy tiles listed
+__global__ void __launch_bounds__(256) scatter_records(Ws w, int T) {
+    const long long nr = min(w.hdr[H_REC], (long long)w.rec_cap);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t r = i0; r < nr; r += stride) {
+        const int4 rc = w.recs[r];
+        if (rc.x < 0 || rc.x >= T) continue;  // slot of a chunk that overflowed
+        const int pos = w.roff[rc.x] - w.nrec[rc.x] + atomicAdd(w.rfill + rc.x, 1);
+        w.sorted[pos] = make_int2(rc.y, rc.z);
+    }
+    for (int64_t t = i0; t < T; t += stride)
+        if (w.nent[t] >= kHeavy) w.heavy[atomicAdd((unsigned long long*)(w.hdr + H_HEAVY), 1ull)] = (int)t;
+}
+
+__global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, Ws w, int32_t* __restrict__ bitset) {
+    extern __shared__ uint32_t sm_bits[];
+    const int TW = 1 << g.twl, TH = 1 << g.thl, TPX = TW * TH, S = g.S;
+    const int rowstride = TPX + 1;
+    __shared__ int s_item;
+    __shared__ int wb[32];
+    const bool vec4 = (S & 3) == 0;
+    const int n_heavy = (int)w.hdr[H_HEAVY];
+    const int items = n_heavy + g.num_tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (int)atomicAdd((unsigned long long*)(w.hdr + H_WORK), 1ull);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= items) break;
+        int tile;
+        if (item < n_heavy) {
+            tile = w.heavy[item];
+        } else {
+            tile = item - n_heavy;
+            if (w.nent[tile] >= kHeavy) continue;  // done among the heavy ones
+        }
+        const int tx = tile % g.tiles_x;
+        const int ty = (tile / g.tiles_x) % g.tiles_y;
+        const int b = tile / (g.tiles_x * g.tiles_y);
+        const int h0 = ty * TH, w0 = tx * TW;
+        const int rows = min(TH, g.H - h0), cols = min(TW, g.W - w0);
+        const int nrec = w.nrec[tile];
+        const int rbeg = w.roff[tile] - nrec;
+        const int64_t row0 = ((int64_t)b * g.H + h0) * g.W + w0;
+        if (nrec == 0) {
+            if (vec4) {
+                const int per_row = cols * (S >> 2);
+                for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
+                    const int r = i / per_row, c = i - r * per_row;
+                    __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W) * S) + c, make_int4(0, 0, 0, 0));
+                }
+            } else {
+                const int per_row = cols * S;
+                for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
+                    const int r = i / per_row, c = i - r * per_row;
+                    __stcs(bitset + (row0 + (int64_t)r * g.W) * S + c, 0);
+                }
+            }
+            continue;
+        }
+        {
+            uint4* z4 = reinterpret_cast<uint4*>(sm_bits);
+            const int n4 = (S * rowstride) >> 2;
+            for (int i = threadIdx.x; i < n4; i += blockDim.x) z4[i] = make_uint4(0, 0, 0, 0);
+            for (int i = (n4 << 2) + threadIdx.x; i < S * rowstride; i += blockDim.x) sm_bits[i] = 0u;
+        }
+        __syncthreads();
+        // one warp per record; the record's entries are contiguous
+        for (int r = warp; r < nrec; r += kRasterThreads / 32) {
+            const int2 rc = w.sorted[rbeg + r];
+            for (int i = lane; i < rc.y; i += 32) {
+                const uint2 e = __ldcs(w.entries + rc.x + i);
+                const int c = e.x & 0xffff;
+                if (c >= 32 * S) continue;
+                uint32_t* col = sm_bits + (size_t)(c >> 5) * rowstride;
+                const uint32_t bit = 1u << (c & 31);
+                const int lp = (e.x >> 16) & 0xfff;
+                int lh = lp >> g.twl, lw = lp & (TW - 1);
+                const int axis = (e.x >> 28) & 1;
+                const int dir = (e.x >> 29) & 1 ? -1 : 1;
+                const int n = (e.y & 31) + 1;
+                const unsigned steps = e.y >> 5;
+                for (int k = 0; k < n; ++k) {
+                    if ((unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW) atomicOr(col + lh * TW + lw, bit);
+                    const int st = (steps >> k) & 1;
+                    if (axis) { lh += 1; lw += st ? dir : 0; }
+                    else { lw += 1; lh += st ? dir : 0; }
+                }
+            }
+        }
+        __syncthreads();
+        if (vec4) {
+            const int G = S >> 2, per_row = cols * G;
+            for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
+                const int r = i / per_row, rem = i - r * per_row;
+                const int px = rem / G, sg = rem - px * G;
+                const uint32_t* src = sm_bits + (size_t)(4 * sg) * rowstride + r * TW + px;
+                __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W + px) * S + 4 * sg),
+                       make_int4((int)src[0], (int)src[rowstride], (int)src[2 * rowstride], (int)src[3 * rowstride]));
+            }
+        } else {
+            const int per_row = cols * S;
+            for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
+                const int r = i / per_row, rem = i - r * per_row;
+                const int px = rem / S, sl = rem - px * S;
+                __stcs(bitset + (row0 + (int64_t)r * g.W) * S + rem, (int)sm_bits[(size_t)sl * rowstride + r * TW + px]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// chunks that did not fit: global atomicOr on the finished bitset
+__global__ void __launch_bounds__(256) dda_fixup_kernel(int64_t P, Lines L, Geo g, const int32_t* __restrict__ p2c,
+                                                        Ws w, int32_t* __restrict__ bitset) {
+    const int64_t noc = min((long long)w.chunk_cap, w.hdr[H_OVER]);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < noc * kChunk; i += stride) {
+        const int64_t p = (int64_t)w.over[i / kChunk] * kChunk + (i % kChunk);
+        Prim q;
+        if (p >= P || !load_prim(p, L, q)) continue;
+        const Span s = dda_span(q.p0, q.p1, g.H, g.W);
+        const int c = cluster_of(p2c, q.e, L.E, g.S, w.hdr + H_BAD);
+        if (c < 0) continue;
+        for (int k = 0; k < s.count; ++k) {
+            float x, y;
+            dda_sample(s, k, x, y);
+            const int h = f2i(floorf(y)), wv = f2i(floorf(x));
+            if (h < 0 || h >= g.H || wv < 0 || wv >= g.W) continue;
+            const float t1 = dda_t1(q.p0, q.p1, x, y, s.axis, g.H, g.W);
+            if (!z_ok(dda_z(q.p0, q.p1, t1))) continue;
+            atomicOr(bitset + (((int64_t)q.b * g.H + h) * g.W + wv) * g.S + (c >> 5), (int32_t)(1u << (c & 31)));
+        }
+    }
+}
+
+static size_t bin_smem() { return (size_t)3 * kHT * 4 + (size_t)(kStage * kBinThreads + kSpill) * (8 + 4); }
+static size_t raster_smem(const Geo& g) { return (size_t)g.S * (((size_t)1 << (g.twl + g.thl)) + 1) * 4; }
+
+}  // namespace s2c
+
+using namespace s2c;
+
+extern "C" size_t s2c_dda_cluster_bitset_workspace_size(int64_t P, int B, int H, int W, int S) {
+    if (B <= 0 || H <= 0 || W <= 0 || S <= 0 || P < 0) return 0;
+    const Geo g = make_geo(B, H, W, S);
+    Ws w;
+    const size_t fixed = layout(nullptr, (size_t)-1, P, g, w);
+    const int64_t entries = 2 * P + (1 << 16);  // ~1.2 runs per hair segment; 2x headroom
+    return fixed + (size_t)entries * sizeof(uint2);
+}
+
+extern "C" s2c_status s2c_dda_cluster_bitset(int64_t P, const int32_t* edge_ids, int H, int W, int B, int V,
+                                             const float* pos, int E, const int32_t* edges, const int32_t* p2c,
+                                             int S, int32_t* bitset, void* ws, size_t ws_bytes, s2c_stream stream) {
+    if (s2c_status s = check_lines(P, edge_ids, H, W, B, V, pos, E, edges, "dda_cluster_bitset")) return s;
+    S2C_REQUIRE(S > 0 && S <= 2048, "dda_cluster_bitset: slot count must be in [1, 2048] (K <= 65536)");
+    S2C_REQUIRE(bitset && ((uintptr_t)bitset & 15) == 0, "dda_cluster_bitset: bitset must be 16-byte aligned");
+    S2C_REQUIRE(P == 0 || p2c, "dda_cluster_bitset: null prim2cluster");
+    const Geo g = make_geo(B, H, W, S);
+    S2C_REQUIRE((int64_t)B * g.tiles_x * g.tiles_y < (1LL << 31), "dda_cluster_bitset: too many tiles");
+    Ws w;
+    const size_t fixed = layout(ws, ws_bytes, P, g, w);
+    if (!ws || ws_bytes < fixed + 4096 * sizeof(uint2)) {
+        set_error("dda_cluster_bitset: workspace too small");
+        return S2C_ERR_WORKSPACE;
+    }
+    const size_t rs = raster_smem(g);
+    S2C_REQUIRE(rs <= 200 * 1024, "dda_cluster_bitset: tile too large for shared memory");
+    cudaStream_t st = (cudaStream_t)stream;
+    static size_t cfg_raster = 0;
+    static bool cfg_bin = false;
+    if (rs > cfg_raster) {
+        cudaFuncSetAttribute(dda_tile_raster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
+        cfg_raster = rs;
+    }
+    if (!cfg_bin) {
+        cudaFuncSetAttribute(dda_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem());
+        cfg_bin = true;
+    }
+    const int T = g.num_tiles;
+    fused_init<<<grid_for(std::max(T, (int)H_WORDS), 256, 2048), 256, 0, st>>>(w.hdr, w.nrec, w.nent, w.rfill, T);
+    S2C_CHECK_LAUNCH("fused_init");
+    const Lines L = make_lines(edge_ids, B, V, pos, E, edges);
+    if (P > 0) {
+        dda_bin_kernel<<<(unsigned)w.chunk_cap, kBinThreads, bin_smem(), st>>>(P, L, g, p2c, w);
+        S2C_CHECK_LAUNCH("dda_bin_kernel");
+    }
+    if (s2c_status s = inclusive_scan_i32(w.nrec, T, w.roff, w.scan_ws, (int64_t*)((char*)w.scan_ws + w.scan_total_off),
+                                          st))
+        return s;
+    scatter_records<<<2 * num_sms(), 256, 0, st>>>(w, T);
+    S2C_CHECK_LAUNCH("scatter_records");
+    static int occ = 0;
+    static size_t occ_rs = 0;
+    if (occ_rs != rs) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dda_tile_raster_kernel, kRasterThreads, rs);
+        occ_rs = rs;
+        if (occ < 1) occ = 1;
+    }
+    const unsigned rgrid = (unsigned)std::min<int64_t>((int64_t)occ * num_sms(), T);
+    dda_tile_raster_kernel<<<rgrid, kRasterThreads, rs, st>>>(g, w, bitset);
+    S2C_CHECK_LAUNCH("dda_tile_raster_kernel");
+    if (P > 0) {
+        dda_fixup_kernel<<<2 * num_sms(), 256, 0, st>>>(P, L, g, p2c, w, bitset);
+        S2C_CHECK_LAUNCH("dda_fixup_kernel");
+    }
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_dda_cluster_bitset_stats(const void* ws, size_t ws_bytes, int64_t* entries,
+                                                   int64_t* overflow_prims) {
+    S2C_REQUIRE(ws && ws_bytes >= H_WORDS * sizeof(long long), "dda_cluster_bitset_stats: bad workspace");
+    long long hdr[H_WORDS];
+    cudaError_t e = cudaMemcpy(hdr, ws, sizeof(hdr), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_status(e, "dda_cluster_bitset_stats");
+    if (entries) *entries = hdr[H_ENT];
+    if (overflow_prims) *overflow_prims = hdr[H_OVER] * kChunk;
+    return S2C_OK;
+}
