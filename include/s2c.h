@@ -102,6 +102,19 @@ S2C_API s2c_status s2c_dda_cluster_bitset(int64_t num_prims, const int32_t* edge
                                   int B, int V, const float* pos, int E, const int32_t* edges,
                                   const int32_t* prim2cluster, int S, int32_t* bitset,
                                   void* workspace, size_t workspace_bytes, s2c_stream stream);
+/* No counterpart in the reference.  s2c_dda_cluster_bitset for callers that cannot
+ * allocate device memory (a plugin inside a host application that owns the device memory
+ * pool and passes only input and output buffers, or a C caller with no allocator): the
+ * scratch is a 32 MiB array inside libs2c.so that every GPU loading the library holds
+ * until the process exits.  Problems whose s2c_dda_cluster_bitset_workspace_size()
+ * exceeds 32 MiB are rejected with S2C_ERR_INVALID (about 1.4M segments at 1024x1024).
+ * No cudaMalloc/cudaFree.  The first call on each device looks up the array's device
+ * address (make it before any stream capture).  All calls share the array, so calls that
+ * overlap on the GPU (different streams, or different host threads) race; serialise them. */
+S2C_API s2c_status s2c_dda_cluster_bitset_noalloc(int64_t num_prims, const int32_t* edge_ids, int H,
+                                                  int W, int B, int V, const float* pos, int E,
+                                                  const int32_t* edges, const int32_t* prim2cluster,
+                                                  int S, int32_t* bitset, s2c_stream stream);
 /* after a call on the same stream (synchronise first): how many primitives took the
  * global-atomic fallback because the workspace or a tile's record list was full */
 S2C_API s2c_status s2c_dda_cluster_bitset_stats(const void* workspace, size_t workspace_bytes,

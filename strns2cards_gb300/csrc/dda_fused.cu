@@ -649,3 +649,63 @@ extern "C" s2c_status s2c_dda_cluster_bitset_stats(const void* ws, size_t ws_byt
     if (overflow_prims) *overflow_prims = hdr[H_OVER] * kChunk;
     return S2C_OK;
 }
+
+// ---------------------------------------------------------------------------------------
+// Fixed-scratch variant: the same fused DDA -> bitset with its scratch in a device array
+// owned by the library, for callers that cannot allocate device memory themselves (for
+// example a plugin running inside a host application that owns the device memory pool
+// and hands it only input and output buffers, or a C caller with no allocator to draw a
+// workspace from).
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace {
+
+constexpr size_t kFixedScratchBytes = size_t(32) << 20;  // 32 MiB per GPU, held until exit
+
+// Every GPU that loads libs2c.so holds this array for the life of the process.
+__device__ __align__(256) unsigned char g_fixed_scratch[kFixedScratchBytes];
+
+std::mutex g_fixed_mu;
+void* g_fixed_ptr[256];  // device address of g_fixed_scratch, per device ordinal
+
+// The host symbol g_fixed_scratch is not a device address; cudaGetSymbolAddress gives the
+// device address, once per device, with that device current.
+s2c_status fixed_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "dda_cluster_bitset_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= 256) {
+        set_error("dda_cluster_bitset_noalloc: device ordinal %d out of range", dev);
+        return S2C_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_fixed_mu);
+    if (!g_fixed_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_fixed_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "dda_cluster_bitset_noalloc: cudaGetSymbolAddress");
+        g_fixed_ptr[dev] = p;
+    }
+    *out = g_fixed_ptr[dev];
+    return S2C_OK;
+}
+
+}  // namespace
+
+extern "C" s2c_status s2c_dda_cluster_bitset_noalloc(int64_t P, const int32_t* edge_ids, int H, int W, int B, int V,
+                                                     const float* pos, int E, const int32_t* edges,
+                                                     const int32_t* p2c, int S, int32_t* bitset,
+                                                     s2c_stream stream) {
+    const size_t need = s2c_dda_cluster_bitset_workspace_size(P, B, H, W, S);
+    if (need > kFixedScratchBytes) {
+        set_error("dda_cluster_bitset_noalloc: this problem needs %zu bytes of scratch, more than the fixed %zu "
+                  "(use s2c_dda_cluster_bitset with a caller workspace)",
+                  need, kFixedScratchBytes);
+        return S2C_ERR_INVALID;
+    }
+    void* scratch = nullptr;
+    if (s2c_status s = fixed_scratch(&scratch)) return s;
+    // the counters the kernels need zeroed are cleared by the first launch of every call
+    return s2c_dda_cluster_bitset(P, edge_ids, H, W, B, V, pos, E, edges, p2c, S, bitset, scratch,
+                                  kFixedScratchBytes, stream);
+}
