@@ -10,7 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/s2c.h"
+#include "s2c.h"
 
 namespace s2c {
 
@@ -47,6 +47,20 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 1 << 30) {
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// n / d for 0 <= n < 2^31 by multiply-high (Granlund & Montgomery, "Division by invariant
+// integers using multiplication", 1994): l = ceil(log2 d), m = 2^32 (2^l - d) / d + 1,
+// q = (mulhi(m, n) + n) >> l.
+struct FastDiv {
+    uint32_t d = 1, m = 0, l = 0;
+    FastDiv() = default;
+    explicit FastDiv(uint32_t dv) : d(dv ? dv : 1) {
+        l = 0;
+        while ((1ull << l) < d) ++l;
+        m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const { return (__umulhi(m, n) + n) >> l; }
+};
+
 // carve aligned sub-buffers out of a caller workspace
 struct Carver {
     char* base;
@@ -74,22 +88,22 @@ struct Span {
     int count;      // fragments before bounds / depth rejection
 };
 
-// Pixel-space endpoint (dda.cu:25-36)
+// Pixel-space endpoint (dda.cu:25-36); Unit: w == 1, where the division is exact and skipped
+template <bool Unit>
 __device__ __forceinline__ void dda_pixel(float4 p, float fW, float fH, float& x, float& y) {
-    // division by w = 1 is exact, so orthographic views skip the two divisions
-    const bool unit = p.w == 1.0f;
-    const float xn = unit ? p.x : __fdiv_rn(p.x, p.w);
-    const float yn = unit ? p.y : __fdiv_rn(p.y, p.w);
+    const float xn = Unit ? p.x : __fdiv_rn(p.x, p.w);
+    const float yn = Unit ? p.y : __fdiv_rn(p.y, p.w);
     x = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(xn, 1.f)), fW);
     y = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(1.f, yn)), fH);
 }
 
-__device__ __forceinline__ Span dda_span(float4 p0, float4 p1, int H, int W) {
+template <bool Unit>
+__device__ __forceinline__ Span dda_span_t(float4 p0, float4 p1, int H, int W) {
     Span s;
     const float fH = (float)H, fW = (float)W;
     float x0, y0, x1, y1;
-    dda_pixel(p0, fW, fH, x0, y0);
-    dda_pixel(p1, fW, fH, x1, y1);
+    dda_pixel<Unit>(p0, fW, fH, x0, y0);
+    dda_pixel<Unit>(p1, fW, fH, x1, y1);
     const float dx = __fsub_rn(x1, x0), dy = __fsub_rn(y1, y0);
     s.sx = s.sy = s.slope = s.off0 = s.off1 = 0.f;
     s.axis = 0.f;
@@ -125,6 +139,13 @@ __device__ __forceinline__ Span dda_span(float4 p0, float4 p1, int H, int W) {
         s.count = c > 0 ? c : 0;
     }
     return s;
+}
+
+// Orthographic views (w = 1 at both ends) take a copy without the four divisions; a real
+// branch, so the divisions are not evaluated and discarded.
+__device__ __forceinline__ Span dda_span(float4 p0, float4 p1, int H, int W) {
+    if (p0.w == 1.0f && p1.w == 1.0f) return dda_span_t<true>(p0, p1, H, W);
+    return dda_span_t<false>(p0, p1, H, W);
 }
 
 // Sample point of fragment k (dda.cu:185-193); the minor coordinate is not fused.

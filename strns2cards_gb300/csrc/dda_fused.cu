@@ -240,8 +240,8 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
                 const int last = s.count - 1;
                 auto sample = [&](int k, int& im, int& in) {
                     const float d = fminf(fmaxf(__fadd_rn((float)k, 0.5f), s.off0), s.off1);
-                    im = f2i(floorf(__fadd_rn(smaj, d)));
-                    in = f2i(floorf(__fadd_rn(smin, __fmul_rn(d, s.slope))));
+                    im = __float2int_rd(__fadd_rn(smaj, d));
+                    in = __float2int_rd(__fadd_rn(smin, __fmul_rn(d, s.slope)));
                 };
                 int m0, n0, ml, nl;
                 sample(0, m0, n0);
@@ -249,41 +249,69 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
                 // Simple sweep: every fragment passes the depth test, both end fragments are
                 // inside the image (coordinates are monotonic in k, so all are), and the
                 // major pixel is start + k (exact for interior samples d = k + 0.5; checked
-                // at both ends).  Then only the minor coordinate needs evaluating.
-                const bool simple = zfast && isfinite(s.slope) && m0 == f2i(smaj) && ml == m0 + last &&
-                                    m0 >= 0 && ml < nmaj && min(n0, nl) >= 0 && max(n0, nl) < nmin;
+                // at both ends).  Then only the minor coordinate needs evaluating, and the
+                // interior samples need no clamping (off0 < 1.5 <= k + 0.5 < off1).
+                const int dir = s.slope >= 0.f ? 1 : -1;
+                bool simple = zfast && isfinite(s.slope) && last <= 32 && m0 == f2i(smaj) && ml == m0 + last &&
+                              m0 >= 0 && ml < nmaj && min(n0, nl) >= 0 && max(n0, nl) < nmin;
+                // Phase 1: one bit per step k-1 -> k: does the minor pixel move?  Interior
+                // samples are d = k + 0.5 exactly; the last fragment was sampled above.
+                uint32_t bits = 0;
                 if (simple) {
-                    const int dir = s.slope >= 0.f ? 1 : -1;
-                    const uint32_t dbit = (uint32_t)(dir < 0) << 29;
-                    const int TM = 1 << lgmaj;
-                    int kcross = TM - (m0 & (TM - 1));
-                    auto start = [&](int im, int in, int& tile, int& lp) {
-                        const int h = axis ? im : in, wv = axis ? in : im;
-                        tile = (tbase + (h >> g.thl)) * g.tiles_x + (wv >> g.twl);
-                        lp = (h & (TH - 1)) * TW + (wv & (TW - 1));
-                    };
-                    int r_tile, r_lp;
-                    start(m0, n0, r_tile, r_lp);
-                    int r_n = 1, prev = n0;
-                    unsigned r_steps = 0;
-                    for (int k = 1; k <= last; ++k) {
-                        const float d = fminf(fmaxf(__fadd_rn((float)k, 0.5f), s.off0), s.off1);
-                        const int in = f2i(floorf(__fadd_rn(smin, __fmul_rn(d, s.slope))));
+                    int prev = n0;
+                    bool bad = false;
+                    float kf = 1.5f;
+                    for (int k = 1; k < last; ++k, kf += 1.0f) {
+                        const int in = __float2int_rd(__fadd_rn(smin, __fmul_rn(kf, s.slope)));
                         const int dm = in - prev;
-                        if (k == kcross || ((in ^ prev) >> lgmin) != 0 || r_n == kMaxRun || (dm != 0 && dm != dir)) {
-                            emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | dbit,
-                                                    (uint32_t)(r_n - 1) | (r_steps << 5)));
-                            start(m0 + k, in, r_tile, r_lp);
-                            r_n = 1;
-                            r_steps = 0;
-                            if (k == kcross) kcross += TM;
-                        } else {
-                            r_steps |= (uint32_t)(dm != 0) << (r_n - 1);
-                            ++r_n;
-                        }
+                        bits |= (uint32_t)(dm != 0) << (k - 1);
+                        bad |= (dm != 0) & (dm != dir);
                         prev = in;
                     }
-                    emit(r_tile, make_uint2(xbase | ((uint32_t)r_lp << 16) | dbit, (uint32_t)(r_n - 1) | (r_steps << 5)));
+                    if (last > 0) {
+                        const int dm = nl - prev;
+                        bits |= (uint32_t)(dm != 0) << (last - 1);
+                        bad |= (dm != 0) & (dm != dir);
+                    }
+                    simple = !bad;
+                }
+                if (simple) {
+                    // Phase 2: cut at screen-tile borders and every kMaxRun fragments.
+                    const uint32_t dbit = (uint32_t)(dir < 0) << 29;
+                    const int TM = 1 << lgmaj, TN = 1 << lgmin;
+                    // end of the piece that starts at fragment k0 (tile border, run cap or the end)
+                    auto piece_end = [&](int k0, int mk) {
+                        const int jk = m0 + k0;
+                        int k1 = min(last + 1, min(k0 + kMaxRun, k0 + TM - (jk & (TM - 1))));
+                        const int dist = dir > 0 ? TN - (mk & (TN - 1)) : (mk & (TN - 1)) + 1;
+                        uint32_t ahead = k0 >= 32 ? 0u : bits >> k0;  // bit j: step to fragment k0 + j + 1
+                        if (__popc(ahead) >= dist) {
+                            for (int i = 1; i < dist; ++i) ahead &= ahead - 1u;
+                            k1 = min(k1, k0 + __ffs(ahead));          // first fragment in the next tile
+                        }
+                        return k1;
+                    };
+                    auto emit_piece = [&](int k0, int k1, int mk) {
+                        const int jk = m0 + k0, n = k1 - k0;
+                        const uint32_t steps = (n >= 2) ? ((bits >> k0) & ((1u << (n - 1)) - 1u)) : 0u;
+                        const int h = axis ? jk : mk, wv = axis ? mk : jk;
+                        const int tile = (tbase + (h >> g.thl)) * g.tiles_x + (wv >> g.twl);
+                        const int lp = (h & (TH - 1)) * TW + (wv & (TW - 1));
+                        emit(tile, make_uint2(xbase | ((uint32_t)lp << 16) | dbit, (uint32_t)(n - 1) | (steps << 5)));
+                    };
+                    // The first piece: the whole sweep when both end fragments share a tile
+                    // (coordinates are monotonic, so every fragment does) and it fits one entry.
+                    const bool one = ((m0 ^ ml) >> lgmaj) == 0 && ((n0 ^ nl) >> lgmin) == 0 && last < kMaxRun;
+                    int k1 = one ? last + 1 : piece_end(0, n0);
+                    emit_piece(0, k1, n0);
+                    int k0 = k1;
+                    while (k0 <= last) {
+                        const uint32_t below = k0 >= 32 ? bits : (bits & ((1u << k0) - 1u));
+                        const int mk = n0 + dir * __popc(below);  // minor pixel of fragment k0
+                        k1 = piece_end(k0, mk);
+                        emit_piece(k0, k1, mk);
+                        k0 = k1;
+                    }
                 } else {
                     // general sweep: every fragment tested as in the reference
                     int r_n = 0, r_tile = -1, r_lp = 0, r_dir = 0, r_lh = 0, r_lw = 0;
@@ -445,8 +473,7 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
     extern __shared__ uint32_t sm_bits[];
     const int TW = 1 << g.twl, TH = 1 << g.thl, TPX = TW * TH, S = g.S;
     const int rowstride = TPX + 1;
-    __shared__ int s_item;
-    __shared__ int wb[32];
+    __shared__ int s_item, s_rec;
     const bool vec4 = (S & 3) == 0;
     const int n_heavy = (int)w.hdr[H_HEAVY];
     const int items = n_heavy + g.num_tiles;
@@ -474,17 +501,26 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
         const int rbeg = w.roff[tile] - nrec;
         const int64_t row0 = ((int64_t)b * g.H + h0) * g.W + w0;
         if (nrec == 0) {
+            // empty tile: zeros, row by row, 16 bytes per store where possible
             if (vec4) {
                 const int per_row = cols * (S >> 2);
-                for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
-                    const int r = i / per_row, c = i - r * per_row;
+                int r = threadIdx.x / per_row, c = threadIdx.x - r * per_row;
+                const int dr = kRasterThreads / per_row, dc = kRasterThreads - dr * per_row;
+                for (; r < rows;) {
                     __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W) * S) + c, make_int4(0, 0, 0, 0));
+                    r += dr;
+                    c += dc;
+                    if (c >= per_row) { c -= per_row; ++r; }
                 }
             } else {
                 const int per_row = cols * S;
-                for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
-                    const int r = i / per_row, c = i - r * per_row;
+                int r = threadIdx.x / per_row, c = threadIdx.x - r * per_row;
+                const int dr = kRasterThreads / per_row, dc = kRasterThreads - dr * per_row;
+                for (; r < rows;) {
                     __stcs(bitset + (row0 + (int64_t)r * g.W) * S + c, 0);
+                    r += dr;
+                    c += dc;
+                    if (c >= per_row) { c -= per_row; ++r; }
                 }
             }
             continue;
@@ -496,38 +532,97 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             for (int i = (n4 << 2) + threadIdx.x; i < S * rowstride; i += blockDim.x) sm_bits[i] = 0u;
         }
         __syncthreads();
-        // one warp per record; the record's entries are contiguous
-        for (int r = warp; r < nrec; r += kRasterThreads / 32) {
+        // Warps pull records from a shared counter.  Each warp loads 32 entries, scans their
+        // run lengths and lets each lane decode one fragment: major offset i, minor offset
+        // popc(steps & ((1 << i) - 1)) in the run's direction.
+        if (threadIdx.x == 0) s_rec = 0;
+        __syncthreads();
+        for (;;) {
+            int r = 0;
+            if (lane == 0) r = atomicAdd(&s_rec, 1);
+            r = __shfl_sync(0xffffffffu, r, 0);
+            if (r >= nrec) break;
             const int2 rc = w.sorted[rbeg + r];
-            for (int i = lane; i < rc.y; i += 32) {
-                const uint2 e = __ldcs(w.entries + rc.x + i);
+            for (int base = 0; base < rc.y; base += 32) {
+                uint2 e = make_uint2(0, 0);
+                int n = 0;
+                if (base + lane < rc.y) {
+                    e = __ldcs(w.entries + rc.x + base + lane);
+                    n = (int)(e.y & 31) + 1;
+                    if ((int)(e.x & 0xffff) >= 32 * S) n = 0;
+                }
                 const int c = e.x & 0xffff;
-                if (c >= 32 * S) continue;
                 uint32_t* col = sm_bits + (size_t)(c >> 5) * rowstride;
                 const uint32_t bit = 1u << (c & 31);
+                const int axis = (e.x >> 28) & 1, dir = (e.x >> 29) & 1 ? -1 : 1;
                 const int lp = (e.x >> 16) & 0xfff;
-                int lh = lp >> g.twl, lw = lp & (TW - 1);
-                const int axis = (e.x >> 28) & 1;
-                const int dir = (e.x >> 29) & 1 ? -1 : 1;
-                const int n = (e.y & 31) + 1;
                 const unsigned steps = e.y >> 5;
-                for (int k = 0; k < n; ++k) {
-                    if ((unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW) atomicOr(col + lh * TW + lw, bit);
-                    const int st = (steps >> k) & 1;
-                    if (axis) { lh += 1; lw += st ? dir : 0; }
-                    else { lw += 1; lh += st ? dir : 0; }
+                // fragments 0..3 of this lane's run
+                {
+                    int lh = lp >> g.twl, lw = lp & (TW - 1);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        if (i < n && (unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW)
+                            atomicOr(col + lh * TW + lw, bit);
+                        const int st = (steps >> i) & 1;
+                        lh += axis ? 1 : (st ? dir : 0);
+                        lw += axis ? (st ? dir : 0) : 1;
+                    }
+                }
+                // fragments 4.. of the longer runs, one per lane across the warp
+                const int rest = n > 4 ? n - 4 : 0;
+                if (__any_sync(0xffffffffu, rest > 0)) {
+                    int incl = rest;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    const int total = __shfl_sync(0xffffffffu, incl, 31);
+                    const int excl = incl - rest;
+                    for (int f0 = 0; f0 < total; f0 += 32) {
+                        const int f = f0 + lane;
+                        int own = 0;  // first lane whose inclusive count exceeds f
+#pragma unroll
+                        for (int step = 16; step; step >>= 1) {
+                            const int v = __shfl_sync(0xffffffffu, incl, own + step - 1);
+                            if (v <= f) own += step;
+                        }
+                        own = min(own, 31);
+                        const int i = 4 + f - __shfl_sync(0xffffffffu, excl, own);
+                        const uint32_t ex = __shfl_sync(0xffffffffu, e.x, own);
+                        const uint32_t ey = __shfl_sync(0xffffffffu, e.y, own);
+                        if (f < total) {
+                            const int cc = ex & 0xffff;
+                            const int lpo = (ex >> 16) & 0xfff;
+                            const int mv = __popc((ey >> 5) & ((1u << i) - 1u)) * ((ex >> 29) & 1 ? -1 : 1);
+                            int lh = lpo >> g.twl, lw = lpo & (TW - 1);
+                            if ((ex >> 28) & 1) { lh += i; lw += mv; }
+                            else { lw += i; lh += mv; }
+                            if ((unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW)
+                                atomicOr(sm_bits + (size_t)(cc >> 5) * rowstride + lh * TW + lw, 1u << (cc & 31));
+                        }
+                    }
                 }
             }
         }
         __syncthreads();
         if (vec4) {
+            // thread -> (row, pixel, 16-byte slot group), advanced without divisions
             const int G = S >> 2, per_row = cols * G;
-            for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
-                const int r = i / per_row, rem = i - r * per_row;
-                const int px = rem / G, sg = rem - px * G;
+            int r = threadIdx.x / per_row, rem = threadIdx.x - r * per_row;
+            const int dr = kRasterThreads / per_row, drem = kRasterThreads - dr * per_row;
+            int px = rem / G, sg = rem - px * G;
+            const int dpx = drem / G, dsg = drem - dpx * G;
+            for (; r < rows;) {
                 const uint32_t* src = sm_bits + (size_t)(4 * sg) * rowstride + r * TW + px;
                 __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W + px) * S + 4 * sg),
                        make_int4((int)src[0], (int)src[rowstride], (int)src[2 * rowstride], (int)src[3 * rowstride]));
+                r += dr;
+                px += dpx;
+                sg += dsg;
+                if (sg >= G) { sg -= G; ++px; }
+                if (px >= cols) { px -= cols; ++r; }
             }
         } else {
             const int per_row = cols * S;

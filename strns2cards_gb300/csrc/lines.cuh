@@ -16,6 +16,7 @@ struct Lines {
     const int2* __restrict__ edges2;       // (E) vertex pairs
     int E, V;
     int64_t BE;                            // B * E
+    FastDiv divE;
 };
 
 // Loads primitive p.  Ids outside [0, B*E) and vertex indices outside [0, V) (which the
@@ -23,8 +24,9 @@ struct Lines {
 __device__ __forceinline__ bool load_prim(int64_t p, const Lines& L, Prim& q) {
     const int64_t eid = L.edge_ids ? (int64_t)__ldg(L.edge_ids + p) : p;
     if (eid < 0 || eid >= L.BE) return false;
-    q.b = (int)(eid / L.E);
-    q.e = (int)(eid - (int64_t)q.b * L.E);
+    // eid < 2^31 here (edge ids are int32 and primitive counts are capped at 2^31 - 1)
+    q.b = L.BE == L.E ? 0 : (int)L.divE.div((uint32_t)eid);
+    q.e = (int)eid - q.b * L.E;
     const int2 ev = __ldg(L.edges2 + q.e);
     if ((unsigned)ev.x >= (unsigned)L.V || (unsigned)ev.y >= (unsigned)L.V) return false;
     const int64_t vb = (int64_t)q.b * L.V;
@@ -41,6 +43,7 @@ inline Lines make_lines(const int32_t* edge_ids, int B, int V, const float* pos,
     L.E = E;
     L.V = V;
     L.BE = (int64_t)B * E;
+    L.divE = FastDiv((uint32_t)(E > 0 ? E : 1));
     return L;
 }
 
