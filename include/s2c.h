@@ -121,6 +121,61 @@ S2C_API s2c_status s2c_dda_cluster_bitset_stats(const void* workspace, size_t wo
                                         int64_t* entries, int64_t* overflow_prims);
 
 /* ---------------------------------------------------------------------------------- *
+ * triangle rasterisation and attribute interpolation                                  *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: compute_triangle_rects (pystrns2cards.cpp:245-281; rasterize.cu:9-88).
+ * rects int32 (B*T, 4) = (h0, h_len, w0, w_len); prefix = inclusive scan of h_len*w_len;
+ * total to *num_frags (host, synchronising) when non-NULL. */
+S2C_API size_t s2c_compute_triangle_rects_workspace_size(int B, int T);
+S2C_API s2c_status s2c_compute_triangle_rects(int H, int W, int B, int V, const float* pos, int T,
+                                              const int32_t* tri, int32_t* rects, int32_t* prefix,
+                                              void* workspace, size_t workspace_bytes,
+                                              int64_t* num_frags, s2c_stream stream);
+
+/* replaces: compute_fragments (pystrns2cards.cpp:283-326; rasterize.cu:90-195).
+ * frag_pix pre-filled with -1; covered pixels get (b, y, x) and (b0, b1, z, t + 1). */
+S2C_API s2c_status s2c_compute_fragments(int H, int W, int B, int V, const float* pos, int T,
+                                         const int32_t* tri, const int32_t* prefix,
+                                         const int32_t* rects, int64_t num_frags, int32_t* frag_pix,
+                                         float* frag_attrs, s2c_stream stream);
+
+/* replaces: depth_test (pystrns2cards.cpp:328-356; rasterize.cu:198-278).
+ * rast_out (B, H, W, 4) must be zeroed by the caller (as rasterize.py:55-95 does); pixels
+ * with fragments get the attributes of the nearest one (ties: first in fragment order). */
+S2C_API size_t s2c_depth_test_workspace_size(int B, int H, int W);
+S2C_API s2c_status s2c_depth_test(int B, int H, int W, int64_t num_frags, const int32_t* frag_pix,
+                                  const float* frag_attrs, float* rast_out, void* workspace,
+                                  size_t workspace_bytes, s2c_stream stream);
+
+/* replaces: interpolate_triangle_attributes (pystrns2cards.cpp:394-415; rasterize.cu:367-455).
+ * image (B, H, W, C) pre-zeroed by the caller. */
+S2C_API s2c_status s2c_interpolate_triangle_attributes(int B, int H, int W, int C, const float* rast,
+                                                       int V, const float* attr, int T,
+                                                       const int32_t* tri, float* image,
+                                                       s2c_stream stream);
+
+/* replaces: backward_interpolate_triangle_attributes (pystrns2cards.cpp:417-438;
+ * rasterize.cu:402-472).  d_attr (V, C) accumulated with float atomics. */
+S2C_API s2c_status s2c_backward_interpolate_triangle_attributes(int B, int H, int W, int C,
+                                                                const float* rast,
+                                                                const float* d_image, int T,
+                                                                const int32_t* tri, int V,
+                                                                float* d_attr, s2c_stream stream);
+
+/* replaces: dda_interpolate_attributes (pystrns2cards.cpp:613-647; dda.cu:258-298) */
+S2C_API s2c_status s2c_dda_interpolate_attributes(int B, int H, int W, int C, const float* rast,
+                                                  int V, const float* attr, int E,
+                                                  const int32_t* edges, float* image,
+                                                  s2c_stream stream);
+
+/* replaces: backward_dda_interpolate_attributes (pystrns2cards.cpp:649-680; dda.cu:300-342) */
+S2C_API s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int W, int C,
+                                                           const float* rast, const float* d_image,
+                                                           int E, const int32_t* edges, int V,
+                                                           float* d_attr, s2c_stream stream);
+
+/* ---------------------------------------------------------------------------------- *
  * stream compaction                                                                   *
  * ---------------------------------------------------------------------------------- */
 

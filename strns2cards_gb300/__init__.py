@@ -4,7 +4,9 @@ The public ops keep the names and contracts of the reference package ``pystrns2c
 so that ``import strns2cards_gb300 as s2c`` replaces ``import pystrns2cards as s2c``.
 """
 from .bitset_utils import accumulate_bitset_rgb, popcount_bitset  # noqa: F401
-from .dda import dda_cluster_bitset, dda_compute_fragments  # noqa: F401
+from .dda import (DDAInterpolateAttributes, dda_cluster_bitset, dda_compute_fragments,  # noqa: F401
+                  dda_interpolate_attributes)
 from .mesh import build_edges_from_triangles  # noqa: F401
-from .rasterize import cluster_mask_from_fragments  # noqa: F401
+from .rasterize import (InterpolateTriangleAttributes, cluster_mask_from_fragments, compute_fragments,  # noqa: F401
+                        depth_test, interpolate_triangle_attributes, rasterize)
 from . import _core  # noqa: F401

@@ -124,6 +124,116 @@ def cluster_mask_from_fragments(frag_pix, frag_attrs, prim2cluster, bitset) -> N
          prim2cluster.shape[0], B, H, W, S, ptr(bitset), _stream(bitset))
 
 
+# ---- triangles (pystrns2cards.cpp:245-438) --------------------------------------------
+def compute_triangle_rects(H, W, pos, tri, triangle_rects, frag_prefix_sum) -> int:
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(triangle_rects, _i32, 2, 4, "triangle_rects")
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _cuda(pos, tri, triangle_rects, frag_prefix_sum, msg="All tensors must be CUDA tensors (device_id >= 0).")
+    B, V, _ = pos.shape
+    T = tri.shape[0]
+    if triangle_rects.shape[0] != B * T:
+        raise RuntimeError("`triangle_rects` must have shape [B * T, 4].")
+    if frag_prefix_sum.shape[0] != B * T:
+        raise RuntimeError("`frag_prefix_sum` must have shape [B * T].")
+    L = _lib.lib()
+    ws = workspace(L.s2c_compute_triangle_rects_workspace_size(B, T), pos.device)
+    n = _lib.i64_out()
+    call("s2c_compute_triangle_rects", int(H), int(W), B, V, ptr(pos), T, ptr(tri), ptr(triangle_rects),
+         ptr(frag_prefix_sum), ptr(ws), ws.numel(), ctypes.byref(n), _stream(pos))
+    return int(n.value)
+
+
+def compute_fragments(H, W, pos, tri, frag_prefix_sum, triangle_rects, frag_pix, frag_attrs) -> None:
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _arr(triangle_rects, _i32, 2, 4, "triangle_rects")
+    _arr(frag_pix, _i32, 2, 3, "frag_pix")
+    _arr(frag_attrs, _f32, 2, 4, "frag_attrs")
+    _cuda(pos, tri, frag_prefix_sum, triangle_rects, frag_pix, frag_attrs,
+          msg="All tensors must be CUDA tensors (device_id >= 0).")
+    B, V, _ = pos.shape
+    T = tri.shape[0]
+    F = frag_pix.shape[0]
+    if frag_attrs.shape[0] != F or frag_prefix_sum.shape[0] != B * T:
+        raise RuntimeError("Mismatch in fragment count or prefix sum length.")
+    call("s2c_compute_fragments", int(H), int(W), B, V, ptr(pos), T, ptr(tri), ptr(frag_prefix_sum),
+         ptr(triangle_rects), F, ptr(frag_pix), ptr(frag_attrs), _stream(pos))
+
+
+def depth_test(H, W, frag_pix, frag_attrs, rast_out) -> None:
+    _arr(frag_pix, _i32, 2, 3, "frag_pix")
+    _arr(frag_attrs, _f32, 2, 4, "frag_attrs")
+    _arr(rast_out, _f32, 4, 4, "rast_out")
+    _cuda(frag_pix, frag_attrs, rast_out, msg="All tensors must be on a CUDA device (device_id >= 0)")
+    F = frag_pix.shape[0]
+    B = rast_out.shape[0]
+    if frag_attrs.shape[0] != F:
+        raise RuntimeError("frag_attrs must match frag_pix in size.")
+    if rast_out.shape[1] != H or rast_out.shape[2] != W:
+        raise RuntimeError("rast_out must have shape (B, H, W, 4).")
+    L = _lib.lib()
+    ws = workspace(L.s2c_depth_test_workspace_size(B, int(H), int(W)), rast_out.device)
+    call("s2c_depth_test", B, int(H), int(W), F, ptr(frag_pix), ptr(frag_attrs), ptr(rast_out), ptr(ws), ws.numel(),
+         _stream(rast_out))
+
+
+def interpolate_triangle_attributes(rast, attr, tri, image) -> None:
+    _arr(rast, _f32, 4, 4, "rast")
+    _arr(attr, _f32, 2, name="attr")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(image, _f32, 4, name="image")
+    _cuda(rast, attr, tri, image, msg="All tensors must be on a CUDA device")
+    B, H, W, _ = rast.shape
+    V, C = attr.shape
+    call("s2c_interpolate_triangle_attributes", B, H, W, C, ptr(rast), V, ptr(attr), tri.shape[0], ptr(tri), ptr(image),
+         _stream(rast))
+
+
+def backward_interpolate_triangle_attributes(rast, d_image, tri, d_attr) -> None:
+    _arr(rast, _f32, 4, 4, "rast")
+    _arr(d_image, _f32, 4, name="d_image")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(d_attr, _f32, 2, name="d_attr")
+    _cuda(rast, d_image, tri, d_attr, msg="All tensors must be on a CUDA device")
+    B, H, W, _ = rast.shape
+    V, C = d_attr.shape
+    call("s2c_backward_interpolate_triangle_attributes", B, H, W, C, ptr(rast), ptr(d_image), tri.shape[0], ptr(tri), V,
+         ptr(d_attr), _stream(rast))
+
+
+def dda_interpolate_attributes(rast_dda, attr, edges, image) -> None:
+    _arr(rast_dda, _f32, 4, 4, "rast_dda")
+    _arr(attr, _f32, 2, name="attr")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(image, _f32, 4, name="image")
+    _cuda(rast_dda, attr, edges, image, msg="All arrays must be CUDA tensors.")
+    B, H, W, _ = rast_dda.shape
+    V, C = attr.shape
+    if tuple(image.shape) != (B, H, W, C):
+        raise RuntimeError("image must have shape [B, H, W, C]")
+    call("s2c_dda_interpolate_attributes", B, H, W, C, ptr(rast_dda), V, ptr(attr), edges.shape[0], ptr(edges),
+         ptr(image), _stream(rast_dda))
+
+
+def backward_dda_interpolate_attributes(rast_dda, d_image, edges, d_attr) -> None:
+    _arr(rast_dda, _f32, 4, 4, "rast_dda")
+    _arr(d_image, _f32, 4, name="d_image")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(d_attr, _f32, 2, name="d_attr")
+    _cuda(rast_dda, d_image, edges, d_attr, msg="All tensors must be on CUDA.")
+    B, H, W, _ = rast_dda.shape
+    C = d_image.shape[3]
+    if tuple(d_image.shape[:3]) != (B, H, W):
+        raise RuntimeError("`d_image` must have shape [B, H, W, C] matching rast_dda")
+    if d_attr.shape[1] != C:
+        raise RuntimeError("`d_attr` must have shape [V, C] where C matches d_image.shape(3)")
+    call("s2c_backward_dda_interpolate_attributes", B, H, W, C, ptr(rast_dda), ptr(d_image), edges.shape[0], ptr(edges),
+         d_attr.shape[0], ptr(d_attr), _stream(rast_dda))
+
+
 # ---- bitsets (pystrns2cards.cpp:480-529) ---------------------------------------------
 def accumulate_bitset_rgb(bitset, cluster_rgb, accum_color) -> None:
     _arr(bitset, _i32, 4, name="bitset")

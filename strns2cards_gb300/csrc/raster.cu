@@ -1,0 +1,368 @@
+// Triangle rasterisation, depth test and attribute interpolation (the reference's
+// rasterize.cu:9-472 and dda.cu:258-342), entry for entry, with the same FP32 arithmetic:
+// coverage, barycentrics, depth and triangle ids are bit-identical to the reference.
+//
+// Depth test: the reference keeps, per pixel, the minimum of (bits(z + 2) << 32 | fragment
+// index) with a 64-bit atomicMin (rasterize.cu:198-229); the fragment index there is the
+// position after a compaction whose order depends on block scheduling.  Here the
+// compaction keeps input order, so exact depth ties resolve to the first fragment in
+// (view, triangle, row-major pixel) order, deterministically.
+#include "common.cuh"
+#include "scan.cuh"
+
+namespace s2c {
+
+struct Tris {
+    const float4* __restrict__ pos4;  // (B, V)
+    const int* __restrict__ tri;      // (T, 3)
+    int V, T;
+    FastDiv divT;
+};
+
+// rasterize.cu:9-59: screen rectangle of triangle (b, t)
+__global__ void __launch_bounds__(256) tri_rects_kernel(int H, int W, int B, Tris R, int4* __restrict__ rects,
+                                                        int32_t* __restrict__ counts) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)B * R.T) return;
+    const int b = (int)R.divT.div((uint32_t)idx);
+    const int t = (int)idx - b * R.T;
+    const float fH = (float)H, fW = (float)W;
+    float x0 = fW, y0 = fH, x1 = 0.f, y1 = 0.f;
+    bool bad = false;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int v = __ldg(R.tri + 3 * t + i);
+        if ((unsigned)v >= (unsigned)R.V) { bad = true; continue; }
+        const float4 p = __ldg(R.pos4 + (int64_t)b * R.V + v);
+        const float inv_w = __fdiv_rn(1.f, p.w);
+        const float x = __fmul_rn(__fmul_rn(0.5f, __fmaf_rn(p.x, inv_w, 1.f)), fW);
+        const float y = __fmul_rn(__fmul_rn(0.5f, __fmaf_rn(-p.y, inv_w, 1.f)), fH);
+        x0 = isnan(x) ? x0 : fminf(x, x0);
+        x1 = isnan(x) ? x1 : fmaxf(x, x1);
+        y0 = isnan(y) ? y0 : fminf(y, y0);
+        y1 = isnan(y) ? y1 : fmaxf(y, y1);
+    }
+    const int h0 = max(f2i(floorf(y0)), 0);
+    const int h1 = min(f2i(floorf(y1)), H - 1) + 1;
+    const int w0 = max(f2i(floorf(x0)), 0);
+    const int w1 = min(f2i(floorf(x1)), W - 1) + 1;
+    int hl = (int)((unsigned)h1 - (unsigned)h0), wl = (int)((unsigned)w1 - (unsigned)w0);
+    hl = hl > 0 ? hl : 0;
+    wl = wl > 0 ? wl : 0;
+    if (bad) hl = wl = 0;  // vertex index out of range: the reference would read out of bounds
+    rects[idx] = make_int4(h0, hl, w0, wl);
+    counts[idx] = (int32_t)((uint32_t)hl * (uint32_t)wl);
+}
+
+// Coverage of pixel (x, y) by a triangle with clip-space corners P0..P2
+// (rasterize.cu:132-163).  Returns true and (b0, b1, z) when covered.
+__device__ __forceinline__ bool tri_cover(int H, int W, float4 P0, float4 P1, float4 P2, int x, int y, float& b0,
+                                          float& b1, float& z) {
+    const float px = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)x, 0.5f)), (float)W));
+    const float py = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)y, 0.5f)), (float)H));
+    const float q0x = __fmaf_rn(-px, P0.w, P0.x), q0y = __fmaf_rn(-py, P0.w, -P0.y);
+    const float q1x = __fmaf_rn(-px, P1.w, P1.x), q1y = __fmaf_rn(-py, P1.w, -P1.y);
+    const float q2x = __fmaf_rn(-px, P2.w, P2.x), q2y = __fmaf_rn(-py, P2.w, -P2.y);
+    // a*b - c*d is fused on its first product
+    const float A0 = __fmaf_rn(q1x, q2y, -__fmul_rn(q1y, q2x));
+    const float A1 = __fmaf_rn(q2x, q0y, -__fmul_rn(q2y, q0x));
+    const float A2 = __fmaf_rn(q0x, q1y, -__fmul_rn(q0y, q1x));
+    const float A = __fadd_rn(__fadd_rn(A0, A1), A2);
+    if (A == 0.f) return false;
+    const float invA = __fdiv_rn(1.f, A);
+    b0 = __fmul_rn(A0, invA);
+    b1 = __fmul_rn(A1, invA);
+    // (A0 z0 + A1 z1) + A2 z2 and the same for w, with the reference build's fusion shapes
+    const float zc = __fmaf_rn(A2, P2.z, __fmaf_rn(A1, P1.z, __fmul_rn(A0, P0.z)));
+    const float wc = __fmaf_rn(A2, P2.w, __fmaf_rn(A0, P0.w, __fmul_rn(A1, P1.w)));
+    z = __fdiv_rn(zc, wc);
+    if (!isfinite(b0) || !isfinite(b1) || !isfinite(z)) return false;
+    if (b0 < 0.f || b1 < 0.f || __fadd_rn(b0, b1) > 1.f || z < -1.f || z > 1.f) return false;
+    return true;
+}
+
+// rasterize.cu:90-172: one thread per bounding-box pixel, owner triangle by binary search
+__global__ void __launch_bounds__(256) tri_fragments_kernel(int H, int W, Tris R, int64_t BT, int64_t F,
+                                                            const int32_t* __restrict__ prefix,
+                                                            const int4* __restrict__ rects,
+                                                            int32_t* __restrict__ frag_pix,
+                                                            float4* __restrict__ frag_attrs) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= F) return;
+    int64_t lo = 0, hi = BT;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if ((int64_t)(uint32_t)__ldg(prefix + mid) <= idx) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo >= BT) return;
+    const int b = (int)R.divT.div((uint32_t)lo);
+    const int t = (int)lo - b * R.T;
+    const int4 rc = __ldg(rects + lo);
+    if (rc.w <= 0 || rc.y <= 0) return;
+    const int local = (int)(idx - (lo ? (int64_t)(uint32_t)__ldg(prefix + lo - 1) : 0));
+    const int y = rc.x + local / rc.w;
+    const int x = rc.z + local % rc.w;
+    if (x < 0 || x >= W || y < 0 || y >= H) return;
+    const int i0 = __ldg(R.tri + 3 * t), i1 = __ldg(R.tri + 3 * t + 1), i2 = __ldg(R.tri + 3 * t + 2);
+    if ((unsigned)i0 >= (unsigned)R.V || (unsigned)i1 >= (unsigned)R.V || (unsigned)i2 >= (unsigned)R.V) return;
+    const float4* pb = R.pos4 + (int64_t)b * R.V;
+    float b0, b1, z;
+    if (!tri_cover(H, W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z)) return;
+    frag_pix[3 * idx] = b;
+    frag_pix[3 * idx + 1] = y;
+    frag_pix[3 * idx + 2] = x;
+    frag_attrs[idx] = make_float4(b0, b1, z, (float)(t + 1));
+}
+
+// keys are stored as (signed key) ^ 2^63 so that unsigned atomicMin orders them like the
+// reference's signed long long; the empty value LLONG_MAX maps to all ones
+__global__ void fill_keys(unsigned long long* __restrict__ keys, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = 0xffffffffffffffffull;
+}
+
+// rasterize.cu:209-229 (keys compared as signed 64-bit, as the reference's long long;
+// z + 2 > 0 for every accepted fragment, so the unsigned compare orders them the same)
+__global__ void __launch_bounds__(256) depth_keys_kernel(int64_t F, const int32_t* __restrict__ frag_pix,
+                                                         const float4* __restrict__ frag_attrs, int B, int H, int W,
+                                                         unsigned long long* __restrict__ keys) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F) return;
+    const int b = frag_pix[3 * i], h = frag_pix[3 * i + 1], w = frag_pix[3 * i + 2];
+    if (b < 0 || b >= B || h < 0 || h >= H || w < 0 || w >= W) return;
+    const float zz = __fadd_rn(frag_attrs[i].z, 2.f);
+    // the reference's signed key (bits(z + 2) << 32) | index, as a bit pattern, mapped to an
+    // order-preserving unsigned value
+    const unsigned long long key = ((unsigned long long)(uint32_t)__float_as_int(zz) << 32) | (uint32_t)i;
+    const unsigned long long ukey = key ^ 0x8000000000000000ull;
+    atomicMin(keys + ((int64_t)b * H + h) * W + w, ukey);
+}
+
+__global__ void __launch_bounds__(256) depth_gather_kernel(int64_t npix, const unsigned long long* __restrict__ keys,
+                                                           const float4* __restrict__ frag_attrs, int64_t F,
+                                                           float4* __restrict__ rast) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const unsigned long long k = keys[p] ^ 0x8000000000000000ull;
+    if (k == 0xffffffffffffffffull) return;  // no fragment (the fill value)
+    const int fi = (int)(uint32_t)(k & 0xffffffffull);
+    if (fi < 0 || fi >= F) return;
+    rast[p] = frag_attrs[fi];
+}
+
+// rasterize.cu:367-400
+__global__ void __launch_bounds__(256) interp_kernel(int64_t npix, const float4* __restrict__ rast, int C,
+                                                     const float* __restrict__ attr, int V,
+                                                     const int* __restrict__ tri, int T, float* __restrict__ image) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float4 r = rast[p];
+    const int t = f2i(r.w) - 1;
+    if (t < 0 || t >= T) return;
+    const float b0 = r.x, b1 = r.y, b2 = __fsub_rn(__fsub_rn(1.f, b0), b1);
+    const int v0 = __ldg(tri + 3 * t), v1 = __ldg(tri + 3 * t + 1), v2 = __ldg(tri + 3 * t + 2);
+    if ((unsigned)v0 >= (unsigned)V || (unsigned)v1 >= (unsigned)V || (unsigned)v2 >= (unsigned)V) return;
+    const float* a0 = attr + (int64_t)C * v0;
+    const float* a1 = attr + (int64_t)C * v1;
+    const float* a2 = attr + (int64_t)C * v2;
+    for (int d = 0; d < C; ++d)
+        image[p * C + d] = __fmaf_rn(b2, __ldg(a2 + d), __fmaf_rn(b1, __ldg(a1 + d), __fmul_rn(b0, __ldg(a0 + d))));
+}
+
+// rasterize.cu:402-438: scatter-add of grad * b_i (float atomics, as the reference)
+__global__ void __launch_bounds__(256) interp_backward_kernel(int64_t npix, const float4* __restrict__ rast, int C,
+                                                              const float* __restrict__ d_image,
+                                                              const int* __restrict__ tri, int T, int V,
+                                                              float* __restrict__ d_attr) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float4 r = rast[p];
+    const int t = f2i(r.w) - 1;
+    if (t < 0 || t >= T) return;
+    const float b0 = r.x, b1 = r.y, b2 = __fsub_rn(__fsub_rn(1.f, b0), b1);
+    const int v0 = __ldg(tri + 3 * t), v1 = __ldg(tri + 3 * t + 1), v2 = __ldg(tri + 3 * t + 2);
+    if ((unsigned)v0 >= (unsigned)V || (unsigned)v1 >= (unsigned)V || (unsigned)v2 >= (unsigned)V) return;
+    for (int d = 0; d < C; ++d) {
+        const float g = d_image[p * C + d];
+        atomicAdd(d_attr + (int64_t)C * v0 + d, __fmul_rn(g, b0));
+        atomicAdd(d_attr + (int64_t)C * v1 + d, __fmul_rn(g, b1));
+        atomicAdd(d_attr + (int64_t)C * v2 + d, __fmul_rn(g, b2));
+    }
+}
+
+// dda.cu:258-284
+__global__ void __launch_bounds__(256) dda_interp_kernel(int64_t npix, const float4* __restrict__ rast, int C,
+                                                         const float* __restrict__ attr, int V,
+                                                         const int2* __restrict__ edges, int E,
+                                                         float* __restrict__ image) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float4 r = rast[p];
+    const int e = f2i(r.w) - 1;
+    if (e < 0 || e >= E) return;
+    const float t1 = r.y, t0 = __fsub_rn(1.f, t1);
+    const int2 ev = __ldg(edges + e);
+    if ((unsigned)ev.x >= (unsigned)V || (unsigned)ev.y >= (unsigned)V) return;
+    for (int d = 0; d < C; ++d)
+        image[p * C + d] = __fmaf_rn(t1, __ldg(attr + (int64_t)C * ev.y + d), __fmul_rn(t0, __ldg(attr + (int64_t)C * ev.x + d)));
+}
+
+// dda.cu:300-327
+__global__ void __launch_bounds__(256) dda_interp_backward_kernel(int64_t npix, const float4* __restrict__ rast, int C,
+                                                                  const float* __restrict__ d_image,
+                                                                  const int2* __restrict__ edges, int E, int V,
+                                                                  float* __restrict__ d_attr) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npix) return;
+    const float4 r = rast[p];
+    const int e = f2i(r.w) - 1;
+    if (e < 0 || e >= E) return;
+    const float t1 = r.y, t0 = __fsub_rn(1.f, t1);
+    const int2 ev = __ldg(edges + e);
+    if ((unsigned)ev.x >= (unsigned)V || (unsigned)ev.y >= (unsigned)V) return;
+    for (int d = 0; d < C; ++d) {
+        const float g = d_image[p * C + d];
+        atomicAdd(d_attr + (int64_t)C * ev.x + d, __fmul_rn(g, t0));
+        atomicAdd(d_attr + (int64_t)C * ev.y + d, __fmul_rn(g, t1));
+    }
+}
+
+}  // namespace s2c
+
+using namespace s2c;
+
+static Tris make_tris(int V, const float* pos, int T, const int32_t* tri) {
+    Tris R;
+    R.pos4 = (const float4*)pos;
+    R.tri = tri;
+    R.V = V;
+    R.T = T;
+    R.divT = FastDiv((uint32_t)(T > 0 ? T : 1));
+    return R;
+}
+
+extern "C" size_t s2c_compute_triangle_rects_workspace_size(int B, int T) {
+    return scan_workspace_bytes((int64_t)B * T) + 256;
+}
+
+extern "C" s2c_status s2c_compute_triangle_rects(int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
+                                                 int32_t* rects, int32_t* prefix, void* ws, size_t ws_bytes,
+                                                 int64_t* num_frags, s2c_stream stream) {
+    S2C_REQUIRE(H > 0 && W > 0 && B > 0 && V >= 0 && T >= 0, "compute_triangle_rects: bad sizes");
+    const int64_t BT = (int64_t)B * T;
+    S2C_REQUIRE(BT < (1LL << 31), "compute_triangle_rects: B*T too large");
+    S2C_REQUIRE(BT == 0 || (pos && tri && rects && prefix), "compute_triangle_rects: null pointer");
+    S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && ((uintptr_t)rects & 15) == 0, "compute_triangle_rects: misaligned");
+    if (!ws || ws_bytes < s2c_compute_triangle_rects_workspace_size(B, T)) {
+        set_error("compute_triangle_rects: workspace too small");
+        return S2C_ERR_WORKSPACE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t* d_total = (int64_t*)((char*)ws + scan_workspace_bytes(BT));
+    if (BT > 0) {
+        tri_rects_kernel<<<grid_for(BT, 256), 256, 0, st>>>(H, W, B, make_tris(V, pos, T, tri), (int4*)rects, prefix);
+        S2C_CHECK_LAUNCH("tri_rects_kernel");
+    }
+    if (s2c_status s = inclusive_scan_i32(prefix, BT, prefix, ws, d_total, st)) return s;
+    if (s2c_status s = read_count(d_total, num_frags, st)) return s;
+    if (num_frags && *num_frags > 0x7fffffffLL) {
+        set_error("compute_triangle_rects: %lld bounding-box pixels exceed the int32 prefix sum", (long long)*num_frags);
+        return S2C_ERR_INVALID;
+    }
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_compute_fragments(int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
+                                            const int32_t* prefix, const int32_t* rects, int64_t F, int32_t* frag_pix,
+                                            float* frag_attrs, s2c_stream stream) {
+    S2C_REQUIRE(H > 0 && W > 0 && B > 0 && V >= 0 && T >= 0 && F >= 0, "compute_fragments: bad sizes");
+    if (F == 0 || (int64_t)B * T == 0) return S2C_OK;
+    S2C_REQUIRE(pos && tri && prefix && rects && frag_pix && frag_attrs, "compute_fragments: null pointer");
+    S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && ((uintptr_t)rects & 15) == 0 && ((uintptr_t)frag_attrs & 15) == 0,
+                "compute_fragments: misaligned");
+    tri_fragments_kernel<<<grid_for(F, 256), 256, 0, (cudaStream_t)stream>>>(
+        H, W, make_tris(V, pos, T, tri), (int64_t)B * T, F, prefix, (const int4*)rects, frag_pix, (float4*)frag_attrs);
+    S2C_CHECK_LAUNCH("tri_fragments_kernel");
+    return S2C_OK;
+}
+
+extern "C" size_t s2c_depth_test_workspace_size(int B, int H, int W) { return (size_t)B * H * W * 8 + 256; }
+
+extern "C" s2c_status s2c_depth_test(int B, int H, int W, int64_t F, const int32_t* frag_pix, const float* frag_attrs,
+                                     float* rast_out, void* ws, size_t ws_bytes, s2c_stream stream) {
+    S2C_REQUIRE(B > 0 && H > 0 && W > 0 && F >= 0, "depth_test: bad sizes");
+    S2C_REQUIRE(F < (1LL << 31), "depth_test: too many fragments");
+    S2C_REQUIRE(rast_out && ((uintptr_t)rast_out & 15) == 0, "depth_test: rast_out must be 16-byte aligned");
+    S2C_REQUIRE(F == 0 || (frag_pix && frag_attrs && ((uintptr_t)frag_attrs & 15) == 0), "depth_test: bad fragments");
+    if (!ws || ws_bytes < s2c_depth_test_workspace_size(B, H, W)) {
+        set_error("depth_test: workspace too small");
+        return S2C_ERR_WORKSPACE;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t npix = (int64_t)B * H * W;
+    unsigned long long* keys = (unsigned long long*)ws;
+    fill_keys<<<grid_for(npix, 256), 256, 0, st>>>(keys, npix);
+    if (F > 0)
+        depth_keys_kernel<<<grid_for(F, 256), 256, 0, st>>>(F, frag_pix, (const float4*)frag_attrs, B, H, W, keys);
+    depth_gather_kernel<<<grid_for(npix, 256), 256, 0, st>>>(npix, keys, (const float4*)frag_attrs, F, (float4*)rast_out);
+    S2C_CHECK_LAUNCH("depth_test");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_interpolate_triangle_attributes(int B, int H, int W, int C, const float* rast, int V,
+                                                          const float* attr, int T, const int32_t* tri, float* image,
+                                                          s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && T >= 0, "interpolate_triangle_attributes: bad sizes");
+    const int64_t npix = (int64_t)B * H * W;
+    if (npix == 0 || C == 0) return S2C_OK;
+    S2C_REQUIRE(rast && attr && tri && image && ((uintptr_t)rast & 15) == 0, "interpolate_triangle_attributes: bad pointer");
+    interp_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(npix, (const float4*)rast, C, attr, V, tri, T,
+                                                                         image);
+    S2C_CHECK_LAUNCH("interp_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_backward_interpolate_triangle_attributes(int B, int H, int W, int C, const float* rast,
+                                                                   const float* d_image, int T, const int32_t* tri,
+                                                                   int V, float* d_attr, s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && T >= 0,
+                "backward_interpolate_triangle_attributes: bad sizes");
+    const int64_t npix = (int64_t)B * H * W;
+    if (npix == 0 || C == 0) return S2C_OK;
+    S2C_REQUIRE(rast && d_image && tri && d_attr && ((uintptr_t)rast & 15) == 0,
+                "backward_interpolate_triangle_attributes: bad pointer");
+    interp_backward_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(npix, (const float4*)rast, C, d_image,
+                                                                                  tri, T, V, d_attr);
+    S2C_CHECK_LAUNCH("interp_backward_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_dda_interpolate_attributes(int B, int H, int W, int C, const float* rast, int V,
+                                                     const float* attr, int E, const int32_t* edges, float* image,
+                                                     s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && E >= 0, "dda_interpolate_attributes: bad sizes");
+    const int64_t npix = (int64_t)B * H * W;
+    if (npix == 0 || C == 0) return S2C_OK;
+    S2C_REQUIRE(rast && attr && edges && image && ((uintptr_t)rast & 15) == 0 && ((uintptr_t)edges & 7) == 0,
+                "dda_interpolate_attributes: bad pointer");
+    dda_interp_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(npix, (const float4*)rast, C, attr, V,
+                                                                             (const int2*)edges, E, image);
+    S2C_CHECK_LAUNCH("dda_interp_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int W, int C, const float* rast,
+                                                              const float* d_image, int E, const int32_t* edges, int V,
+                                                              float* d_attr, s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && E >= 0,
+                "backward_dda_interpolate_attributes: bad sizes");
+    const int64_t npix = (int64_t)B * H * W;
+    if (npix == 0 || C == 0) return S2C_OK;
+    S2C_REQUIRE(rast && d_image && edges && d_attr && ((uintptr_t)rast & 15) == 0 && ((uintptr_t)edges & 7) == 0,
+                "backward_dda_interpolate_attributes: bad pointer");
+    dda_interp_backward_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(
+        npix, (const float4*)rast, C, d_image, (const int2*)edges, E, V, d_attr);
+    S2C_CHECK_LAUNCH("dda_interp_backward_kernel");
+    return S2C_OK;
+}

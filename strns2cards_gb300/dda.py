@@ -59,6 +59,43 @@ def dda_compute_fragments(
     return pix_out[:n], attrs_out[:n]
 
 
+class DDAInterpolateAttributes(torch.autograd.Function):
+    """``dda.py:79-120``: image = (1 - t1) a[v0] + t1 a[v1] per pixel of a line raster."""
+
+    @staticmethod
+    def forward(ctx, rast: torch.Tensor, attr: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
+        if not rast.is_cuda or not attr.is_cuda or not edges.is_cuda:
+            raise ValueError("All input tensors must be CUDA tensors.")
+        if rast.dtype != torch.float32 or attr.dtype != torch.float32:
+            raise ValueError("`rast` and `attr` must be float32.")
+        if edges.dtype != torch.int32:
+            raise ValueError("`edges` must be int32.")
+        if rast.ndim != 4 or rast.shape[-1] != 4:
+            raise ValueError("`rast` must have shape (B, H, W, 4).")
+        if attr.ndim != 2:
+            raise ValueError("`attr` must have shape (V, C).")
+        if edges.ndim != 2 or edges.shape[1] != 2:
+            raise ValueError("`edges` must have shape (E, 2).")
+        B, H, W, _ = rast.shape
+        V, C = attr.shape
+        image = torch.zeros((B, H, W, C), dtype=torch.float32, device=rast.device)
+        _core.dda_interpolate_attributes(rast.contiguous(), attr.contiguous(), edges.contiguous(), image)
+        ctx.save_for_backward(rast, attr, edges)
+        return image
+
+    @staticmethod
+    def backward(ctx, d_image: torch.Tensor):
+        rast, attr, edges = ctx.saved_tensors
+        d_attr = torch.zeros_like(attr)
+        _core.backward_dda_interpolate_attributes(rast.contiguous(), d_image.contiguous(), edges.contiguous(), d_attr)
+        return None, d_attr, None
+
+
+def dda_interpolate_attributes(rast: torch.Tensor, attr: torch.Tensor, edges: torch.Tensor) -> torch.Tensor:
+    """Differentiable interpolation of per-vertex attributes along rasterised lines (``dda.py:123-136``)."""
+    return DDAInterpolateAttributes.apply(rast, attr, edges)
+
+
 def dda_cluster_bitset(
     resolution: Tuple[int, int],
     pos: torch.Tensor,

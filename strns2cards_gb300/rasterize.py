@@ -8,6 +8,95 @@ import torch
 from . import _core
 
 
+def compute_fragments(
+    resolution: Tuple[int, int],
+    pos: torch.Tensor,
+    tri: torch.Tensor,
+) -> Tuple[torch.Tensor, torch.Tensor]:
+    """Triangle fragments (``rasterize.py:6-53``): ``frag_pix`` (N, 3) int32 = (view, row, col),
+    ``frag_attrs`` (N, 4) float32 = (b0, b1, z, triangle_id + 1), in (view, triangle,
+    row-major pixel) order."""
+    H, W = resolution
+    if not pos.is_cuda or not tri.is_cuda:
+        raise ValueError("Input tensors must be on CUDA.")
+    if pos.dtype != torch.float32 or tri.dtype != torch.int32:
+        raise ValueError("`pos` must be float32 and `tri` must be int32.")
+    if pos.ndim != 3 or pos.shape[2] != 4:
+        raise ValueError("`pos` must have shape (B, V, 4).")
+    if tri.ndim != 2 or tri.shape[1] != 3:
+        raise ValueError("`tri` must have shape (T, 3).")
+    if not pos.is_contiguous() or not tri.is_contiguous():
+        raise ValueError("Input tensors must be contiguous.")
+    B = pos.shape[0]
+    T = tri.shape[0]
+    dev = pos.device
+    rects = torch.empty((B * T, 4), dtype=torch.int32, device=dev)
+    prefix = torch.empty((B * T,), dtype=torch.int32, device=dev)
+    F = _core.compute_triangle_rects(H, W, pos, tri, rects, prefix)
+    frag_pix = torch.full((F, 3), -1, dtype=torch.int32, device=dev)
+    frag_attrs = torch.empty((F, 4), dtype=torch.float32, device=dev)
+    _core.compute_fragments(H, W, pos, tri, prefix, rects, frag_pix, frag_attrs)
+    pix_out = torch.empty_like(frag_pix)
+    attrs_out = torch.empty_like(frag_attrs)
+    n = _core.filter_valid_fragments(frag_pix, frag_attrs, pix_out, attrs_out)
+    return pix_out[:n], attrs_out[:n]
+
+
+def depth_test(B: int, resolution: Tuple[int, int], frag_pix: torch.Tensor, frag_attrs: torch.Tensor) -> torch.Tensor:
+    """Nearest fragment per pixel (``rasterize.py:55-95``): (B, H, W, 4) float32, zeros where empty."""
+    if not (frag_pix.is_cuda and frag_attrs.is_cuda):
+        raise ValueError("Input tensors must be on CUDA.")
+    if frag_pix.dtype != torch.int32:
+        raise ValueError("frag_pix must be int32.")
+    if frag_attrs.dtype != torch.float32:
+        raise ValueError("frag_attrs must be float32.")
+    if frag_pix.ndim != 2 or frag_pix.shape[1] != 3:
+        raise ValueError("frag_pix must have shape (N, 3).")
+    if frag_attrs.ndim != 2 or frag_attrs.shape[1] != 4:
+        raise ValueError("frag_attrs must have shape (N, 4).")
+    if frag_pix.shape[0] != frag_attrs.shape[0]:
+        raise ValueError("frag_pix and frag_attrs must match in length.")
+    H, W = resolution
+    rast = torch.zeros((B, H, W, 4), dtype=torch.float32, device=frag_pix.device)
+    _core.depth_test(H, W, frag_pix.contiguous(), frag_attrs.contiguous(), rast)
+    return rast
+
+
+def rasterize(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:
+    """``compute_fragments`` then ``depth_test`` (``rasterize.py:97-116``)."""
+    frag_pix, frag_attrs = compute_fragments(resolution, pos, tri)
+    return depth_test(pos.shape[0], resolution, frag_pix, frag_attrs)
+
+
+class InterpolateTriangleAttributes(torch.autograd.Function):
+    """``rasterize.py:119-147``: image = b0 a0 + b1 a1 + (1 - b0 - b1) a2; the backward
+    scatters grad * b_i to the vertex attributes."""
+
+    @staticmethod
+    def forward(ctx, rast: torch.Tensor, attr: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:
+        if not (rast.is_cuda and attr.is_cuda and tri.is_cuda):
+            raise ValueError("All inputs must be CUDA tensors.")
+        B, H, W, _ = rast.shape
+        V, C = attr.shape
+        image = torch.zeros((B, H, W, C), dtype=attr.dtype, device=attr.device)
+        _core.interpolate_triangle_attributes(rast.contiguous(), attr.contiguous(), tri.contiguous(), image)
+        ctx.save_for_backward(rast, tri, attr)
+        return image
+
+    @staticmethod
+    def backward(ctx, grad_output: torch.Tensor):
+        rast, tri, attr = ctx.saved_tensors
+        d_attr = torch.zeros_like(attr)
+        _core.backward_interpolate_triangle_attributes(rast.contiguous(), grad_output.contiguous(), tri.contiguous(),
+                                                       d_attr)
+        return None, d_attr, None
+
+
+def interpolate_triangle_attributes(rast: torch.Tensor, attr: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:
+    """Differentiable barycentric interpolation of per-vertex attributes (``rasterize.py:150-167``)."""
+    return InterpolateTriangleAttributes.apply(rast, attr, tri)
+
+
 def cluster_mask_from_fragments(
     resolution: Tuple[int, int],
     frag_pix: torch.Tensor,
