@@ -199,6 +199,37 @@ S2C_API s2c_status s2c_accumulate_bitset_rgb(int64_t num_pixels, int S, const in
                                      int num_clusters, const float* cluster_rgb,
                                      float* accum_color, s2c_stream stream);
 
+/* new: the XOR-popcount loss of antialias.py:124-126 (popcount_bitset(a ^ b).sum()) in
+ * one pass; *total (device uint64) = sum over nwords int32 words of popc(a ^ b). */
+S2C_API s2c_status s2c_xor_popcount(int64_t nwords, const int32_t* a, const int32_t* b,
+                                    uint64_t* total, s2c_stream stream);
+
+/* new: per-cluster pixel counts for the per-card bitset IoU: inter[c] = #pixels with bit c
+ * set in both bitsets, uni[c] = #pixels with bit c set in either (device uint64, K each). */
+S2C_API s2c_status s2c_cluster_iou_counts(int64_t num_pixels, int S, int K, const int32_t* a,
+                                          const int32_t* b, uint64_t* inter, uint64_t* uni,
+                                          s2c_stream stream);
+
+/* ---------------------------------------------------------------------------------- *
+ * antialiased cluster bitset loss                                                     *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: mark_discontinuity_edges (pystrns2cards.cpp:682-715; antialias.cu:38-119).
+ * prim_ids (B*E) pre-filled with -1 and normals (B*E, 2) zeroed by the caller; silhouette
+ * and boundary edges get prim_ids[b*E+e] = b*E+e and an oriented unit normal. */
+S2C_API s2c_status s2c_mark_discontinuity_edges(int H, int W, int B, int V, const float* pos, int T,
+                                                const int32_t* tri, int E, const int32_t* edges,
+                                                const int32_t* edge2tri, int32_t* prim_ids,
+                                                float* normals, s2c_stream stream);
+
+/* replaces: backward_antialiased_cluster_bitset (pystrns2cards.cpp:717-772; antialias.cu:121-317).
+ * d_pos (B, V, 4) accumulated (x, y, w components) from the silhouette-edge fragments. */
+S2C_API s2c_status s2c_backward_antialiased_cluster_bitset(
+    int64_t num_frags, const int32_t* frag_pix, const float* frag_attrs, int B, int H, int W, int S,
+    const int32_t* bitset, const int32_t* target, int V, const float* pos, int E,
+    const int32_t* edges, const float* normals, const int32_t* edge2cluster, float* d_pos,
+    float kernel_radius, float rho, s2c_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

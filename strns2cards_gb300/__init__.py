@@ -3,7 +3,9 @@
 The public ops keep the names and contracts of the reference package ``pystrns2cards``
 so that ``import strns2cards_gb300 as s2c`` replaces ``import pystrns2cards as s2c``.
 """
-from .bitset_utils import accumulate_bitset_rgb, popcount_bitset  # noqa: F401
+from .antialias import (antialiased_cluster_bitset_grad, antialiased_cluster_bitset_loss,  # noqa: F401
+                        mark_discontinuity_edges)
+from .bitset_utils import accumulate_bitset_rgb, cluster_iou, popcount_bitset, xor_error  # noqa: F401
 from .dda import (DDAInterpolateAttributes, dda_cluster_bitset, dda_compute_fragments,  # noqa: F401
                   dda_interpolate_attributes)
 from .mesh import build_edges_from_triangles  # noqa: F401

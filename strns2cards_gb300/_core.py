@@ -258,6 +258,57 @@ def popcount_bitset(bitset, count_image) -> None:
     call("s2c_popcount_bitset", B * H * W, S, ptr(bitset), ptr(count_image), _stream(bitset))
 
 
+# ---- antialias (pystrns2cards.cpp:682-772) --------------------------------------------
+def mark_discontinuity_edges(H, W, tri, edges, edge2tri, pos, prim_ids, normals) -> None:
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(edge2tri, _i32, 2, 2, "edge2tri")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(prim_ids, _i32, 1, name="prim_ids")
+    _arr(normals, _f32, 2, 2, "normals")
+    _cuda(tri, edges, edge2tri, pos, prim_ids, normals, msg="mark_discontinuity_edges: all input tensors must be CUDA.")
+    B, V, _ = pos.shape
+    E = edges.shape[0]
+    if edge2tri.shape[0] != E:
+        raise RuntimeError("mark_discontinuity_edges: edge2tri must have the same number of edges.")
+    if prim_ids.shape[0] != B * E:
+        raise RuntimeError("mark_discontinuity_edges: prim_ids must have shape (B * E).")
+    if normals.shape[0] != B * E:
+        raise RuntimeError("mark_discontinuity_edges: normals must have shape (B * E, 2).")
+    call("s2c_mark_discontinuity_edges", int(H), int(W), B, V, ptr(pos), tri.shape[0], ptr(tri), E, ptr(edges),
+         ptr(edge2tri), ptr(prim_ids), ptr(normals), _stream(pos))
+
+
+def backward_antialiased_cluster_bitset(frag_pix, frag_attrs_dda, bitset, target_bitset, pos, edges, normals,
+                                        edge2cluster, d_pos, kernel_radius, rho) -> None:
+    _arr(frag_pix, _i32, 2, 3, "frag_pix")
+    _arr(frag_attrs_dda, _f32, 2, 4, "frag_attrs_dda")
+    _arr(bitset, _i32, 4, name="bitset")
+    _arr(target_bitset, _i32, 4, name="target_bitset")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(normals, _f32, 2, 2, "normals")
+    _arr(edge2cluster, _i32, 1, name="edge2cluster")
+    _arr(d_pos, _f32, 3, 4, "d_pos")
+    _cuda(frag_pix, frag_attrs_dda, bitset, target_bitset, pos, edges, normals, edge2cluster, d_pos,
+          msg="backward_antialiased_bitset: all input tensors must be CUDA.")
+    F = frag_pix.shape[0]
+    B, H, W, S = bitset.shape
+    V = pos.shape[1]
+    E = edges.shape[0]
+    if frag_attrs_dda.shape[0] != F:
+        raise RuntimeError("backward_antialiased_bitset: frag_pix and frag_attrs_dda must match in number of fragments.")
+    if tuple(target_bitset.shape) != (B, H, W, S):
+        raise RuntimeError("backward_antialiased_bitset: target_bitset must match bitset shape.")
+    if d_pos.shape[0] != B or d_pos.shape[1] != V:
+        raise RuntimeError("backward_antialiased_bitset: d_pos must match pos shape.")
+    if edge2cluster.shape[0] < E or normals.shape[0] < B * E or pos.shape[0] < B:
+        raise RuntimeError("backward_antialiased_bitset: edge2cluster / normals / pos too short.")
+    call("s2c_backward_antialiased_cluster_bitset", F, ptr(frag_pix), ptr(frag_attrs_dda), B, H, W, S, ptr(bitset),
+         ptr(target_bitset), V, ptr(pos), E, ptr(edges), ptr(normals), ptr(edge2cluster), ptr(d_pos),
+         float(kernel_radius), float(rho), _stream(pos))
+
+
 # ---- compaction (pystrns2cards.cpp:774-786) ------------------------------------------
 def compact_valid_ints(input, output) -> int:
     _arr(input, _i32, 1, name="input")
@@ -276,6 +327,30 @@ def compact_valid_ints(input, output) -> int:
 
 
 # ---- fused entries (no reference counterpart) ----------------------------------------
+def xor_popcount(a, b) -> torch.Tensor:
+    """Device uint64 (as int64) total of popc(a ^ b) over two equal-shape int32 bitsets."""
+    _arr(a, _i32, name="a")
+    _arr(b, _i32, name="b")
+    _cuda(a, b)
+    if a.shape != b.shape:
+        raise RuntimeError("xor_popcount: bitsets must have the same shape.")
+    out = torch.empty(1, dtype=torch.int64, device=a.device)
+    call("s2c_xor_popcount", a.numel(), ptr(a), ptr(b), ptr(out), _stream(a))
+    return out
+
+
+def cluster_iou_counts(a, b, K) -> tuple:
+    _arr(a, _i32, 4, name="a")
+    _arr(b, _i32, 4, name="b")
+    _cuda(a, b)
+    if a.shape != b.shape:
+        raise RuntimeError("cluster_iou_counts: bitsets must have the same shape.")
+    B, H, W, S = a.shape
+    inter = torch.empty(K, dtype=torch.int64, device=a.device)
+    uni = torch.empty(K, dtype=torch.int64, device=a.device)
+    call("s2c_cluster_iou_counts", B * H * W, S, int(K), ptr(a), ptr(b), ptr(inter), ptr(uni), _stream(a))
+    return inter, uni
+
 def dda_cluster_bitset(pos, edges, prim2cluster, bitset, edge_ids=None, ws=None) -> torch.Tensor:
     """Fused DDA -> cluster bitset into ``bitset`` (B, H, W, S), fully overwritten."""
     _arr(pos, _f32, 3, 4, "pos")

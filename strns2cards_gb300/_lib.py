@@ -46,6 +46,11 @@ SIGNATURES = {
     "s2c_backward_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp], c_i),
     "s2c_dda_interpolate_attributes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp], c_i),
     "s2c_backward_dda_interpolate_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp], c_i),
+    "s2c_xor_popcount": ([c_i64, vp, vp, vp, vp], c_i),
+    "s2c_cluster_iou_counts": ([c_i64, c_i, c_i, vp, vp, vp, vp, vp], c_i),
+    "s2c_mark_discontinuity_edges": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, vp], c_i),
+    "s2c_backward_antialiased_cluster_bitset": ([c_i64, vp, vp, c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp, vp,
+                                                 vp, c_f, c_f, vp], c_i),
     "s2c_compact_valid_ints_workspace_size": ([c_i64], c_sz),
     "s2c_compact_valid_ints": ([c_i64, vp, vp, vp, c_sz, i64p, vp], c_i),
     "s2c_popcount_bitset": ([c_i64, c_i, vp, vp, vp], c_i),

@@ -32,3 +32,17 @@ def popcount_bitset(bitset: torch.Tensor) -> torch.Tensor:
     out = torch.zeros((B, H, W), dtype=torch.float32, device=bitset.device)
     _core.popcount_bitset(bitset.contiguous(), out)
     return out
+
+
+def xor_error(bitset: torch.Tensor, target_bitset: torch.Tensor) -> torch.Tensor:
+    """Number of mismatching (pixel, cluster) bits as a float32 scalar: the
+    ``count_xor_error`` loss of ``antialias.py:124-126`` in one pass."""
+    return _core.xor_popcount(bitset.contiguous(), target_bitset.contiguous()).to(torch.float32)[0]
+
+
+def cluster_iou(bitset: torch.Tensor, target_bitset: torch.Tensor, cluster_count: int):
+    """Per-cluster (per-card) bitset IoU: |pred_k & target_k| / |pred_k | target_k| over
+    pixels, with the integer intersection and union counts (NaN where the union is 0)."""
+    inter, uni = _core.cluster_iou_counts(bitset.contiguous(), target_bitset.contiguous(), int(cluster_count))
+    iou = inter.to(torch.float64) / uni.to(torch.float64)
+    return iou, inter, uni

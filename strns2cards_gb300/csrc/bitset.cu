@@ -1,4 +1,6 @@
 // Per-pixel bitset reductions (the reference's bitset_utils.cu) and bitset comparisons.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace s2c {
@@ -47,9 +49,111 @@ __global__ void __launch_bounds__(256) accumulate_rgb_kernel(int64_t npix, int S
     out[3 * p + 2] = b;
 }
 
+// sum over all words of popc(a ^ b): the XOR-popcount loss of antialias.py:124-126 in one
+// pass (the reference materialises a ^ b, a float popcount image and its sum)
+__global__ void __launch_bounds__(256) xor_popcount_kernel(int64_t nwords, const int32_t* __restrict__ a,
+                                                           const int32_t* __restrict__ b,
+                                                           unsigned long long* __restrict__ total) {
+    const int64_t n4 = nwords >> 2;
+    const int4* a4 = reinterpret_cast<const int4*>(a);
+    const int4* b4 = reinterpret_cast<const int4*>(b);
+    unsigned long long s = 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+        const int4 x = __ldcs(a4 + i), y = __ldcs(b4 + i);
+        s += __popc(x.x ^ y.x) + __popc(x.y ^ y.y) + __popc(x.z ^ y.z) + __popc(x.w ^ y.w);
+    }
+    for (int64_t i = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride)
+        s += __popc(a[i] ^ b[i]);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ unsigned long long ws[8];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += ws[i];
+        atomicAdd(total, t);
+    }
+}
+
+// per-cluster pixel counts of a & b and a | b (per-card IoU = inter / union)
+__global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, int K, const int32_t* __restrict__ a,
+                                                          const int32_t* __restrict__ b,
+                                                          unsigned long long* __restrict__ inter,
+                                                          unsigned long long* __restrict__ uni, int use_smem) {
+    extern __shared__ unsigned int hist[];  // 2K counters when use_smem
+    if (use_smem) {
+        for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) hist[i] = 0u;
+        __syncthreads();
+    }
+    const int64_t nwords = npix * S;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride) {
+        const uint32_t x = (uint32_t)__ldcs(a + i), y = (uint32_t)__ldcs(b + i);
+        uint32_t u = x | y;
+        if (!u) continue;
+        const uint32_t both = x & y;
+        const int base = (int)(i % S) * 32;
+        while (u) {
+            const int j = __ffs(u) - 1;
+            u &= u - 1;
+            const int c = base + j;
+            if (c >= K) continue;
+            if (use_smem) {
+                atomicAdd(hist + K + c, 1u);
+                if ((both >> j) & 1) atomicAdd(hist + c, 1u);
+            } else {
+                atomicAdd(uni + c, 1ull);
+                if ((both >> j) & 1) atomicAdd(inter + c, 1ull);
+            }
+        }
+    }
+    if (use_smem) {
+        __syncthreads();
+        for (int c = threadIdx.x; c < K; c += blockDim.x) {
+            if (hist[c]) atomicAdd(inter + c, (unsigned long long)hist[c]);
+            if (hist[K + c]) atomicAdd(uni + c, (unsigned long long)hist[K + c]);
+        }
+    }
+}
+
 }  // namespace s2c
 
 using namespace s2c;
+
+extern "C" s2c_status s2c_xor_popcount(int64_t nwords, const int32_t* a, const int32_t* b, uint64_t* total,
+                                       s2c_stream stream) {
+    S2C_REQUIRE(nwords >= 0 && total, "xor_popcount: bad arguments");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(total, 0, sizeof(uint64_t), st);
+    if (e != cudaSuccess) return cuda_status(e, "xor_popcount: memset");
+    if (nwords == 0) return S2C_OK;
+    S2C_REQUIRE(a && b && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0, "xor_popcount: bitsets must be 16-byte aligned");
+    const unsigned grid = (unsigned)std::min<int64_t>((nwords / 4 + 255) / 256 + 1, (int64_t)num_sms() * 8);
+    xor_popcount_kernel<<<grid, 256, 0, st>>>(nwords, a, b, (unsigned long long*)total);
+    S2C_CHECK_LAUNCH("xor_popcount_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_cluster_iou_counts(int64_t npix, int S, int K, const int32_t* a, const int32_t* b,
+                                             uint64_t* inter, uint64_t* uni, s2c_stream stream) {
+    S2C_REQUIRE(npix >= 0 && S > 0 && K >= 0 && K <= 32 * S, "cluster_iou_counts: bad sizes");
+    S2C_REQUIRE(inter && uni, "cluster_iou_counts: null output");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(inter, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(uni, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e != cudaSuccess) return cuda_status(e, "cluster_iou_counts: memset");
+    if (npix == 0 || K == 0) return S2C_OK;
+    S2C_REQUIRE(a && b, "cluster_iou_counts: null input");
+    const size_t smem = (size_t)2 * K * sizeof(unsigned int);
+    const int use_smem = smem <= 48 * 1024;
+    const unsigned grid = (unsigned)std::min<int64_t>((npix * S + 255) / 256, (int64_t)num_sms() * 8);
+    cluster_iou_kernel<<<grid, 256, use_smem ? smem : 0, st>>>(npix, S, K, a, b, (unsigned long long*)inter,
+                                                               (unsigned long long*)uni, use_smem);
+    S2C_CHECK_LAUNCH("cluster_iou_kernel");
+    return S2C_OK;
+}
 
 extern "C" s2c_status s2c_popcount_bitset(int64_t npix, int S, const int32_t* bitset, float* count_image,
                                           s2c_stream stream) {

@@ -1,0 +1,110 @@
+"""GPU parity of the antialiased cluster-bitset loss.
+
+Silhouette decisions and normals are bit-identical to the reference.  The gradient d_pos
+is float: it must agree with the FP64 oracle (same FP32 decisions, FP64 window sums) to
+``|got - ref| <= 1e-5 * max(|ref|, 1e-3 * max|ref|)`` elementwise, and with the reference's
+own (FP32, __expf, atomics) gradient to the same bound.  Bit counts are exact.
+"""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(lib_built):
+    return lib_built
+
+
+def cu(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def np_(t):
+    return t.detach().cpu().numpy()
+
+
+def grad_close(got, ref, tol=1e-5):
+    ref = np.asarray(ref, np.float64)
+    got = np.asarray(got, np.float64)
+    scale = np.maximum(np.abs(ref), 1e-3 * np.abs(ref).max(initial=0.0))
+    ok = np.abs(got - ref) <= tol * scale + 1e-30
+    return bool(ok.all()), float((np.abs(got - ref) / (scale + 1e-30)).max(initial=0.0))
+
+
+def test_mark_discontinuity_edges_bit_exact():
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    a = golden("antialias.npz")
+    H, W = int(a["H"]), int(a["W"])
+    B, E = a["pos"].shape[0], a["edges"].shape[0]
+    ids = torch.full((B * E,), -1, dtype=torch.int32, device="cuda")
+    nrm = torch.zeros((B * E, 2), dtype=torch.float32, device="cuda")
+    _core.mark_discontinuity_edges(H, W, cu(a["tri"]), cu(a["edges"]), cu(a["edge2tri"]), cu(a["pos"]), ids, nrm)
+    assert np.array_equal(np_(ids), a["raw_prim_ids"])
+    assert np.array_equal(np_(nrm), a["normals"])
+    cids, cn = s2c.mark_discontinuity_edges((H, W), cu(a["pos"]), cu(a["tri"]), cu(a["edges"]), cu(a["edge2tri"]))
+    ref = a["raw_prim_ids"]
+    assert np.array_equal(np_(cids), ref[ref >= 0])
+
+
+@pytest.mark.parametrize("tag,kr,rho", [("r7", 7.0, 0.5), ("r3", 3.5, 1.0)])
+def test_antialias_gradient(tag, kr, rho):
+    import strns2cards_gb300 as s2c
+    a = golden("antialias.npz")
+    args = [cu(a[k]) for k in ("bitset", "target", "pos", "tri", "edges", "edge2tri", "edge2cluster")]
+    pos = args[2].clone().requires_grad_(True)
+    args[2] = pos
+    loss = s2c.antialiased_cluster_bitset_loss(*args, kernel_radius=kr, rho=rho)
+    assert float(loss.detach()) == 1.0
+    (2.0 * loss).backward()
+    got = np_(pos.grad) / 2.0
+    ora = O.antialias_grad(a["bitset"], a["target"], a["pos"], a["tri"], a["edges"], a["edge2tri"], a["edge2cluster"],
+                           kr, rho)
+    ok, err = grad_close(got, ora)
+    assert ok, err
+    assert np.array_equal(got != 0, ora != 0)
+    ok, err = grad_close(got, a["d_pos_" + tag])
+    assert ok, err
+
+
+def test_antialias_on_random_scene_matches_oracle():
+    """Cards of a strand scene, two orthographic views and a perspective one, against the
+    strands' target bitset."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    sc = syn.strand_scene(600, 24, per_cluster=12, num_views=2, seed=13)
+    cards = syn.make_cards(sc.strands, 12, 8, 2)
+    H, W, K = 160, 200, 64
+    cpos = syn.project(cards.verts, sc.mvp)
+    edges, e2t = s2c.build_edges_from_triangles(cards.tri)
+    e2c = cards.tri2cluster[e2t[:, 0]].astype(np.int32)
+    tgt = O.dda_cluster_bitset(H, W, sc.pos, sc.edges, sc.edge2cluster, K)
+    bits = O.cluster_mask_from_fragments(H, W, *O.compute_fragments(H, W, cpos, cards.tri), cards.tri2cluster, K, B=2)
+    got = np_(s2c.antialiased_cluster_bitset_grad(cu(bits), cu(tgt), cu(cpos), cu(cards.tri), cu(edges), cu(e2t),
+                                                   cu(e2c), 7.0, 0.5))
+    ora = O.antialias_grad(bits, tgt, cpos, cards.tri, edges, e2t, e2c, 7.0, 0.5)
+    ok, err = grad_close(got, ora)
+    assert ok, err
+    assert np.abs(ora).max() > 0
+
+
+def test_xor_error_and_cluster_iou_exact():
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(4)
+    a = rng.integers(-2 ** 31, 2 ** 31 - 1, size=(2, 33, 41, 3), dtype=np.int64).astype(np.int32)
+    b = a.copy()
+    flip = rng.random(a.shape) < 0.3
+    b[flip] = rng.integers(-2 ** 31, 2 ** 31 - 1, size=int(flip.sum()), dtype=np.int64).astype(np.int32)
+    ref = int(np.unpackbits((a ^ b).view(np.uint8)).sum())
+    assert int(s2c.xor_error(cu(a), cu(b)).item()) == ref
+    K = 90
+    iou, inter, uni = s2c.cluster_iou(cu(a), cu(b), K)
+    au = np.unpackbits(a.view(np.uint8), bitorder="little").reshape(-1, 96)[:, :K]
+    bu = np.unpackbits(b.view(np.uint8), bitorder="little").reshape(-1, 96)[:, :K]
+    assert np.array_equal(np_(inter), (au & bu).sum(0)) and np.array_equal(np_(uni), (au | bu).sum(0))
+    assert np.array_equal(np_(iou), (au & bu).sum(0) / (au | bu).sum(0))
