@@ -34,6 +34,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 NUM_STRANDS, NUM_VERTS, PER_CLUSTER, RES, K = 50_000, 100, 25, 1024, 2048
+# kernels one s2c_dda_cluster_bitset call launches: init, bin, scan (3), scatter, tile raster, fixup
+LAUNCHES_PER_STEP = 8
 METRIC = "Gseg/s DDA+bitset"
 WORKLOAD = (f"dda_cluster_bitset: {NUM_STRANDS}x{NUM_VERTS} synthetic strands "
             f"({NUM_STRANDS * (NUM_VERTS - 1)} segments) -> {RES}x{RES} view, {K} clusters "
@@ -60,7 +62,7 @@ def load_peaks():
 
 
 def load_traffic():
-    p = os.path.join(ROOT, "profiles", "dda_cluster_bitset_cfg2_traffic.json")
+    p = os.path.join(ROOT, "profiles", "dda_cluster_bitset_50kx100_1024sq_k2048_traffic.json")
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("bytes_per_step")
@@ -281,8 +283,8 @@ def run_ours(args):
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,
                              "algorithmic_bytes_per_step": alg, "traffic": traffic,
-                             "kernel": "s2c_dda_cluster_bitset (init + bin + tile raster + fixup launches)"},
-                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": 4 * args.steps,
+                             "kernel": "s2c_dda_cluster_bitset (init, bin, 3-launch scan, scatter, tile raster, fixup)"},
+                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": LAUNCHES_PER_STEP * args.steps,
                 "wall_s": wall}
         print(json.dumps(line), flush=True)
     if ws > 1:

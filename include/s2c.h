@@ -230,6 +230,56 @@ S2C_API s2c_status s2c_backward_antialiased_cluster_bitset(
     const int32_t* edges, const float* normals, const int32_t* edge2cluster, float* d_pos,
     float kernel_radius, float rho, s2c_stream stream);
 
+/* new: the same gradient with each fragment's contribution formed and summed in FP64 in a
+ * caller workspace (B*V*3 doubles), then added once into d_pos: d_pos is then the
+ * correctly-rounded float of a (nearly) exact sum, independent of scheduling, instead of a
+ * float-atomic sum whose cancellation error depends on it. */
+S2C_API size_t s2c_backward_antialiased_cluster_bitset_workspace_size(int B, int V);
+S2C_API s2c_status s2c_backward_antialiased_cluster_bitset_f64(
+    int64_t num_frags, const int32_t* frag_pix, const float* frag_attrs, int B, int H, int W, int S,
+    const int32_t* bitset, const int32_t* target, int V, const float* pos, int E,
+    const int32_t* edges, const float* normals, const int32_t* edge2cluster, float* d_pos,
+    float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream);
+
+/* ---------------------------------------------------------------------------------- *
+ * strand curves                                                                       *
+ * ---------------------------------------------------------------------------------- */
+
+/* new: cumulative arclength of each strand, arclength[s, 0] = 0 and
+ * arclength[s, i] = sum_{k<=i} |x[s,k] - x[s,k-1]| (curve_utils.py:167-180 computes the same
+ * with torch.norm + torch.cumsum). strands (N, V, 3), arclength (N, V). */
+S2C_API s2c_status s2c_compute_arclength(int N, int V, const float* strands, float* arclength,
+                                         s2c_stream stream);
+
+/* replaces: smooth_strands (pystrns2cards.cpp:841-872; curve_utils.cu:24-68,135-147).
+ * out[s, i] = sum_j w_ij x[s, j] / sum_j w_ij over |a_i - a_j| <= 3 beta,
+ * w_ij = exp(-(a_i - a_j)^2 / beta^2); points whose weight sum is <= 1e-6 are written 0
+ * (the reference leaves them at the zero its caller filled in).  arclength may be NULL:
+ * it is then computed in the kernel as s2c_compute_arclength does. */
+S2C_API s2c_status s2c_smooth_strands(int N, int V, const float* strands, const float* arclength,
+                                      float* smoothed_strands, float beta, s2c_stream stream);
+
+/* replaces: skinning (pystrns2cards.cpp:873-915; curve_utils.cu:70-131,149-166).
+ * out[s, i] = sum_j w_ij (R_j (x_i - h_j) + c_j) / sum_j w_ij with the weights of
+ * s2c_smooth_strands; out = x where the weight sum is <= 1e-8.  R (N, V, 3, 3) row-major.
+ * arclength may be NULL (computed in the kernel). */
+S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float* arclength,
+                                const float* handle_strands, const float* canonical_handles,
+                                const float* R, float* skinned_strands, float beta,
+                                s2c_stream stream);
+
+/* ---------------------------------------------------------------------------------- *
+ * card mesh topology (host)                                                           *
+ * ---------------------------------------------------------------------------------- */
+
+/* replaces: build_edges_from_triangles (pystrns2cards.cpp:208-243; mesh_utils.cpp:36-95).
+ * Host memory.  Unique undirected edges stored (min, max), sorted by (min, max) -- the
+ * reference emits them in std::unordered_map order, which is implementation-defined --
+ * and per edge the first two triangles that contain it (-1 where there is none).
+ * edges and edge2tri hold 3*T rows; *num_edges receives the count. */
+S2C_API s2c_status s2c_build_edges_from_triangles(int T, const int32_t* tri, int32_t* edges,
+                                                  int32_t* edge2tri, int64_t* num_edges);
+
 #ifdef __cplusplus
 }
 #endif

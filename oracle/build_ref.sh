@@ -21,5 +21,11 @@ for u in dda rasterize antialias bitset_utils compact_utils curve_utils; do
     pids+=($!)
   fi
 done
+# the reference's host edge builder (mesh_utils.cpp) behind a small C shim, for the CPU tests
+HERE="$(cd "$(dirname "$0")" && pwd)"
+if [ ! -f "$OUT/libref_mesh.so" ] || [ "$SRC/mesh_utils.cpp" -nt "$OUT/libref_mesh.so" ] || [ "$HERE/ref_mesh_shim.cpp" -nt "$OUT/libref_mesh.so" ]; then
+  ( g++ -O2 -std=c++17 -shared -fPIC -I"$SRC" -o "$OUT/libref_mesh.so" "$SRC/mesh_utils.cpp" "$HERE/ref_mesh_shim.cpp" ) &
+  pids+=($!)
+fi
 for p in "${pids[@]}"; do wait "$p"; done
-echo "build_ref.sh: cubins in $OUT"
+echo "build_ref.sh: cubins and libref_mesh.so in $OUT"

@@ -318,3 +318,35 @@ def sort_frags(pix, attrs):
         return pix, attrs
     key = np.lexsort((pix[:, 2], pix[:, 1], attrs[:, 3], pix[:, 0]))
     return pix[key], attrs[key]
+
+
+# ---- mesh topology: mesh_utils.cpp:36-95 (edge set and first-two-triangle adjacency),
+# in the fixed (min, max)-sorted edge order
+def build_edges_from_triangles(tri: np.ndarray) -> Tuple[np.ndarray, np.ndarray]:
+    if not isinstance(tri, np.ndarray):
+        raise TypeError("Input must be a NumPy ndarray.")
+    if tri.dtype != np.int32:
+        raise TypeError("Triangle indices must be int32.")
+    if tri.ndim != 2 or tri.shape[1] != 3:
+        raise ValueError("Input triangle array must have shape (T, 3).")
+    T = tri.shape[0]
+    if T == 0:
+        return np.zeros((0, 2), np.int32), np.zeros((0, 2), np.int32)
+    t64 = tri.astype(np.int64)
+    a = np.stack([t64[:, 0], t64[:, 1], t64[:, 2]], 1).reshape(-1)
+    b = np.stack([t64[:, 1], t64[:, 2], t64[:, 0]], 1).reshape(-1)
+    lo, hi = np.minimum(a, b), np.maximum(a, b)
+    owner = np.repeat(np.arange(T, dtype=np.int64), 3)
+    order = np.lexsort((owner, hi, lo))
+    lo, hi, owner = lo[order], hi[order], owner[order]
+    first = np.ones(lo.shape[0], dtype=bool)
+    first[1:] = (lo[1:] != lo[:-1]) | (hi[1:] != hi[:-1])
+    starts = np.nonzero(first)[0]
+    edges = np.stack([lo[starts], hi[starts]], 1).astype(np.int32)
+    e2t = np.full((starts.shape[0], 2), -1, dtype=np.int32)
+    e2t[:, 0] = owner[starts]
+    nxt = starts + 1
+    has2 = nxt < lo.shape[0]
+    has2[has2] = ~first[nxt[has2]]
+    e2t[has2, 1] = owner[nxt[has2]]
+    return edges, e2t

@@ -304,9 +304,12 @@ def backward_antialiased_cluster_bitset(frag_pix, frag_attrs_dda, bitset, target
         raise RuntimeError("backward_antialiased_bitset: d_pos must match pos shape.")
     if edge2cluster.shape[0] < E or normals.shape[0] < B * E or pos.shape[0] < B:
         raise RuntimeError("backward_antialiased_bitset: edge2cluster / normals / pos too short.")
-    call("s2c_backward_antialiased_cluster_bitset", F, ptr(frag_pix), ptr(frag_attrs_dda), B, H, W, S, ptr(bitset),
-         ptr(target_bitset), V, ptr(pos), E, ptr(edges), ptr(normals), ptr(edge2cluster), ptr(d_pos),
-         float(kernel_radius), float(rho), _stream(pos))
+    # contributions summed in FP64 in a workspace, then added into d_pos once
+    need = _lib.lib().s2c_backward_antialiased_cluster_bitset_workspace_size(B, V)
+    ws = workspace(need, pos.device)
+    call("s2c_backward_antialiased_cluster_bitset_f64", F, ptr(frag_pix), ptr(frag_attrs_dda), B, H, W, S,
+         ptr(bitset), ptr(target_bitset), V, ptr(pos), E, ptr(edges), ptr(normals), ptr(edge2cluster), ptr(d_pos),
+         float(kernel_radius), float(rho), ptr(ws), ws.numel(), _stream(pos))
 
 
 # ---- compaction (pystrns2cards.cpp:774-786) ------------------------------------------
@@ -381,3 +384,71 @@ def dda_cluster_bitset_stats(ws) -> tuple:
     e, o = _lib.i64_out(), _lib.i64_out()
     call("s2c_dda_cluster_bitset_stats", ptr(ws), ws.numel(), ctypes.byref(e), ctypes.byref(o))
     return int(e.value), int(o.value)
+
+
+# ---- mesh topology (pystrns2cards.cpp:208-243) -----------------------------------------
+def build_edges_from_triangles(tri):
+    """Host: unique edges (E, 2) and edge->triangle map (E, 2) of an int32 (T, 3) numpy array,
+    edges sorted by (min, max) vertex (the reference's order is its hash map's)."""
+    import numpy as np
+    tri = np.ascontiguousarray(tri, dtype=np.int32)
+    T = int(tri.shape[0])
+    edges = np.empty((max(3 * T, 1), 2), np.int32)
+    e2t = np.empty((max(3 * T, 1), 2), np.int32)
+    n = _lib.i64_out()
+    call("s2c_build_edges_from_triangles", T, tri.ctypes.data, edges.ctypes.data, e2t.ctypes.data, ctypes.byref(n))
+    E = int(n.value)
+    return edges[:E].copy(), e2t[:E].copy()
+
+
+# ---- strand curves (pystrns2cards.cpp:841-915) -----------------------------------------
+def compute_arclength(strands, arclength) -> None:
+    _arr(strands, _f32, 3, 3, "strands")
+    _arr(arclength, _f32, 2, name="arclength")
+    _cuda(strands, arclength, msg="compute_arclength: All input tensors must be CUDA.")
+    N, V, _ = strands.shape
+    if tuple(arclength.shape) != (N, V):
+        raise RuntimeError("compute_arclength: arclength must match (num_strands, num_points).")
+    call("s2c_compute_arclength", N, V, ptr(strands), ptr(arclength), _stream(strands))
+
+
+def smooth_strands(strands, arclength, smoothed_strands, beta) -> None:
+    """``arclength`` may be None: the kernel then computes it itself."""
+    _arr(strands, _f32, 3, 3, "strands")
+    _arr(smoothed_strands, _f32, 3, 3, "smoothed_strands")
+    if arclength is not None:
+        _arr(arclength, _f32, 2, name="arclength")
+    _cuda(strands, arclength, smoothed_strands, msg="smooth_strands: All input tensors must be CUDA.")
+    N, V, _ = strands.shape
+    if arclength is not None and tuple(arclength.shape) != (N, V):
+        raise RuntimeError("smooth_strands: arclength must match (num_strands, num_points).")
+    if tuple(smoothed_strands.shape) != (N, V, 3):
+        raise RuntimeError("smooth_strands: smoothed_strands must match (num_strands, num_points, 3).")
+    call("s2c_smooth_strands", N, V, ptr(strands), ptr(arclength), ptr(smoothed_strands), float(beta),
+         _stream(strands))
+
+
+def skinning(strands, arclength, handle_strands, canonical_handles, R, skinned_strands, beta) -> None:
+    """``arclength`` may be None: the kernel then computes it itself."""
+    _arr(strands, _f32, 3, 3, "strands")
+    _arr(handle_strands, _f32, 3, 3, "handle_strands")
+    _arr(canonical_handles, _f32, 3, 3, "canonical_handles")
+    _arr(R, _f32, 4, 3, "R")
+    _arr(skinned_strands, _f32, 3, 3, "skinned_strands")
+    if arclength is not None:
+        _arr(arclength, _f32, 2, name="arclength")
+    _cuda(strands, arclength, handle_strands, canonical_handles, R, skinned_strands,
+          msg="skinning: All input tensors must be CUDA.")
+    N, V, _ = strands.shape
+    if arclength is not None and tuple(arclength.shape) != (N, V):
+        raise RuntimeError("skinning: arclength must match (num_strands, num_points).")
+    if tuple(handle_strands.shape) != (N, V, 3):
+        raise RuntimeError("skinning: handle_strands must match (num_strands, num_points, 3).")
+    if tuple(canonical_handles.shape) != (N, V, 3):
+        raise RuntimeError("skinning: canonical_handles must match (num_strands, num_points, 3).")
+    if tuple(R.shape) != (N, V, 3, 3):
+        raise RuntimeError("skinning: R must match (num_strands, num_points, 3, 3).")
+    if tuple(skinned_strands.shape) != (N, V, 3):
+        raise RuntimeError("skinning: skinned_strands must match (num_strands, num_points, 3).")
+    call("s2c_skinning", N, V, ptr(strands), ptr(arclength), ptr(handle_strands), ptr(canonical_handles), ptr(R),
+         ptr(skinned_strands), float(beta), _stream(strands))

@@ -51,10 +51,17 @@ SIGNATURES = {
     "s2c_mark_discontinuity_edges": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, vp], c_i),
     "s2c_backward_antialiased_cluster_bitset": ([c_i64, vp, vp, c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp, vp,
                                                  vp, c_f, c_f, vp], c_i),
+    "s2c_backward_antialiased_cluster_bitset_workspace_size": ([c_i, c_i], c_sz),
+    "s2c_backward_antialiased_cluster_bitset_f64": ([c_i64, vp, vp, c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp,
+                                                     vp, vp, c_f, c_f, vp, c_sz, vp], c_i),
     "s2c_compact_valid_ints_workspace_size": ([c_i64], c_sz),
     "s2c_compact_valid_ints": ([c_i64, vp, vp, vp, c_sz, i64p, vp], c_i),
     "s2c_popcount_bitset": ([c_i64, c_i, vp, vp, vp], c_i),
     "s2c_accumulate_bitset_rgb": ([c_i64, c_i, vp, c_i, vp, vp, vp], c_i),
+    "s2c_compute_arclength": ([c_i, c_i, vp, vp, vp], c_i),
+    "s2c_smooth_strands": ([c_i, c_i, vp, vp, vp, c_f, vp], c_i),
+    "s2c_skinning": ([c_i, c_i, vp, vp, vp, vp, vp, vp, c_f, vp], c_i),
+    "s2c_build_edges_from_triangles": ([c_i, vp, vp, vp, i64p], c_i),
 }
 
 _lib = None

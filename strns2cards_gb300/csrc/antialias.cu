@@ -79,6 +79,7 @@ struct AAArgs {
     const float2* __restrict__ normals;
     const int32_t* __restrict__ e2c;
     float* __restrict__ d_pos;
+    double* __restrict__ acc64;     // non-null: contributions summed in FP64 here instead
     float kr, rho;
 };
 
@@ -157,6 +158,24 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
         if (lane != 0) continue;
         const double dc = (double)c01 * acc;
         if (dc == 0.0) continue;
+        if (A.acc64) {
+            // chain rule and accumulation in FP64 (no cancellation loss across fragments)
+            const double dxd = dc * 0.5 * (double)fW * (double)nrm.x;
+            const double dyd = dc * -0.5 * (double)fH * (double)nrm.y;
+            const double pwd = (double)pw;
+            const double qx = dxd / pwd, qy = dyd / pwd;
+            const double qw = (dxd * (double)px + dyd * (double)py) / (pwd * pwd);
+            if (!isfinite(qx) || !isfinite(qy) || !isfinite(qw)) continue;
+            double* a0 = A.acc64 + ((int64_t)b * A.V + ev.x) * 3;
+            double* a1 = A.acc64 + ((int64_t)b * A.V + ev.y) * 3;
+            atomicAdd(a0 + 0, qx * (double)t0);
+            atomicAdd(a0 + 1, qy * (double)t0);
+            atomicAdd(a0 + 2, qw * (double)t0);
+            atomicAdd(a1 + 0, qx * (double)t1);
+            atomicAdd(a1 + 1, qy * (double)t1);
+            atomicAdd(a1 + 2, qw * (double)t1);
+            continue;
+        }
         const float dcf = (float)dc;
         const float dx = __fmul_rn(__fmul_rn(__fmul_rn(dcf, 0.5f), fW), nrm.x);
         const float dy = __fmul_rn(__fmul_rn(__fmul_rn(dcf, -0.5f), fH), nrm.y);
@@ -171,6 +190,16 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
         atomicAdd(g1 + 0, __fmul_rn(dpx, t1));
         atomicAdd(g1 + 1, __fmul_rn(dpy, t1));
         atomicAdd(g1 + 3, __fmul_rn(dpw, t1));
+    }
+}
+
+// d_pos[v].{x, y, w} += the FP64 sums
+__global__ void aa_finalize_kernel(int64_t n, const double* __restrict__ acc, float* __restrict__ d_pos) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float* g = d_pos + 4 * i;
+        g[0] = __fadd_rn(g[0], (float)acc[3 * i]);
+        g[1] = __fadd_rn(g[1], (float)acc[3 * i + 1]);
+        g[3] = __fadd_rn(g[3], (float)acc[3 * i + 2]);
     }
 }
 
@@ -205,13 +234,11 @@ extern "C" s2c_status s2c_mark_discontinuity_edges(int H, int W, int B, int V, c
     return S2C_OK;
 }
 
-extern "C" s2c_status s2c_backward_antialiased_cluster_bitset(int64_t F, const int32_t* frag_pix,
-                                                              const float* frag_attrs, int B, int H, int W, int S,
-                                                              const int32_t* bitset, const int32_t* target, int V,
-                                                              const float* pos, int E, const int32_t* edges,
-                                                              const float* normals, const int32_t* edge2cluster,
-                                                              float* d_pos, float kernel_radius, float rho,
-                                                              s2c_stream stream) {
+static s2c_status aa_backward(int64_t F, const int32_t* frag_pix, const float* frag_attrs, int B, int H, int W,
+                              int S, const int32_t* bitset, const int32_t* target, int V, const float* pos, int E,
+                              const int32_t* edges, const float* normals, const int32_t* edge2cluster,
+                              float* d_pos, float kernel_radius, float rho, void* ws, size_t ws_bytes,
+                              cudaStream_t stream) {
     S2C_REQUIRE(F >= 0 && B > 0 && H > 0 && W > 0 && S > 0 && V >= 0 && E >= 0,
                 "backward_antialiased_cluster_bitset: bad sizes");
     if (F == 0) return S2C_OK;
@@ -221,6 +248,14 @@ extern "C" s2c_status s2c_backward_antialiased_cluster_bitset(int64_t F, const i
                     ((uintptr_t)edges & 7) == 0,
                 "backward_antialiased_cluster_bitset: misaligned");
     S2C_REQUIRE(kernel_radius >= 0.f && kernel_radius < 1024.f, "backward_antialiased_cluster_bitset: bad kernel_radius");
+    const int64_t BV = (int64_t)B * V;
+    if (ws) {
+        S2C_REQUIRE(((uintptr_t)ws & 7) == 0 && ws_bytes >= (size_t)BV * 3 * sizeof(double),
+                    "backward_antialiased_cluster_bitset: workspace of %zu bytes, need %lld", ws_bytes,
+                    (long long)(BV * 3 * sizeof(double)));
+        cudaError_t e = cudaMemsetAsync(ws, 0, (size_t)BV * 3 * sizeof(double), stream);
+        if (e != cudaSuccess) return cuda_status(e, "backward_antialiased_cluster_bitset: memset");
+    }
     AAArgs A;
     A.F = F;
     A.frag_pix = frag_pix;
@@ -238,10 +273,40 @@ extern "C" s2c_status s2c_backward_antialiased_cluster_bitset(int64_t F, const i
     A.normals = (const float2*)normals;
     A.e2c = edge2cluster;
     A.d_pos = d_pos;
+    A.acc64 = (double*)ws;
     A.kr = kernel_radius;
     A.rho = rho;
     const int64_t warps = std::min<int64_t>(F, (int64_t)num_sms() * 64);
-    aa_backward_kernel<<<grid_for(warps * 32, 256), 256, 0, (cudaStream_t)stream>>>(A);
+    aa_backward_kernel<<<grid_for(warps * 32, 256), 256, 0, stream>>>(A);
     S2C_CHECK_LAUNCH("aa_backward_kernel");
+    if (ws && BV > 0) {
+        aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, stream>>>(BV, (const double*)ws, d_pos);
+        S2C_CHECK_LAUNCH("aa_finalize_kernel");
+    }
     return S2C_OK;
+}
+
+extern "C" s2c_status s2c_backward_antialiased_cluster_bitset(int64_t F, const int32_t* frag_pix,
+                                                              const float* frag_attrs, int B, int H, int W, int S,
+                                                              const int32_t* bitset, const int32_t* target, int V,
+                                                              const float* pos, int E, const int32_t* edges,
+                                                              const float* normals, const int32_t* edge2cluster,
+                                                              float* d_pos, float kernel_radius, float rho,
+                                                              s2c_stream stream) {
+    return aa_backward(F, frag_pix, frag_attrs, B, H, W, S, bitset, target, V, pos, E, edges, normals, edge2cluster,
+                       d_pos, kernel_radius, rho, nullptr, 0, (cudaStream_t)stream);
+}
+
+extern "C" size_t s2c_backward_antialiased_cluster_bitset_workspace_size(int B, int V) {
+    return (size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3 * sizeof(double);
+}
+
+extern "C" s2c_status s2c_backward_antialiased_cluster_bitset_f64(
+    int64_t F, const int32_t* frag_pix, const float* frag_attrs, int B, int H, int W, int S, const int32_t* bitset,
+    const int32_t* target, int V, const float* pos, int E, const int32_t* edges, const float* normals,
+    const int32_t* edge2cluster, float* d_pos, float kernel_radius, float rho, void* workspace,
+    size_t workspace_bytes, s2c_stream stream) {
+    S2C_REQUIRE(workspace, "backward_antialiased_cluster_bitset_f64: null workspace");
+    return aa_backward(F, frag_pix, frag_attrs, B, H, W, S, bitset, target, V, pos, E, edges, normals, edge2cluster,
+                       d_pos, kernel_radius, rho, workspace, workspace_bytes, (cudaStream_t)stream);
 }

@@ -1,0 +1,223 @@
+// Strand curve operators: arclength, Gaussian-in-arclength smoothing, arclength skinning.
+//
+// Reference: curve_utils.cu:24-68 (smooth_strands_kernel) and :70-131 (skinning_kernel), one
+// thread per strand walking all V x V point pairs straight from global memory with a
+// 12-byte stride per thread.  Here a CTA takes a group of whole strands, stages their
+// points (and handles / rotations for skinning) in shared memory with coalesced loads,
+// computes the arclength in the CTA when the caller passes none (a warp scan per strand),
+// and gives every point its own thread, so the O(V^2) pair loop reads broadcast shared
+// memory.  Per point i the sum runs over j = 0..V-1 in order and skips pairs with
+// |a_i - a_j| > 3 beta exactly as the reference does; weights exp(-d^2 / beta^2) use expf.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace s2c {
+namespace {
+
+constexpr int kCurveThreads = 256;
+constexpr int kCurveSmem = 48 * 1024;           // bytes of staged strand data per CTA
+constexpr int kSmoothBytes = 16;                // x(3) + arclength
+constexpr int kSkinBytes = 76;                  // x(3) + arclength + h(3) + c(3) + R(9)
+constexpr int kMaxArcOnly = kCurveSmem / 4;     // longest strand whose arclength fits alone
+
+struct CurveArgs {
+    int N, V, spb, ngroups;
+    bool staged;                                // whole group staged (else only arclength)
+    const float* x;
+    const float* arc;                           // nullable: computed in the kernel
+    const float* h;
+    const float* c;
+    const float* R;
+    float* out;
+    float beta;
+};
+
+// arclength of one strand (points x[0..V), xyz interleaved) into arc[0..V), by one warp:
+// segment lengths, then an inclusive warp scan per 32-point chunk carried across chunks.
+__device__ __forceinline__ void warp_arclength(const float* x, int V, float* arc, int lane) {
+    float carry = 0.f;
+    for (int base = 0; base < V; base += 32) {
+        const int i = base + lane;
+        float d = 0.f;
+        if (i > 0 && i < V) {
+            const float dx = __fsub_rn(x[3 * i], x[3 * i - 3]);
+            const float dy = __fsub_rn(x[3 * i + 1], x[3 * i - 2]);
+            const float dz = __fsub_rn(x[3 * i + 2], x[3 * i - 1]);
+            d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float t = __shfl_up_sync(0xffffffffu, d, o);
+            if (lane >= o) d = __fadd_rn(d, t);
+        }
+        if (i < V) arc[i] = __fadd_rn(carry, d);
+        carry = __fadd_rn(carry, __shfl_sync(0xffffffffu, d, 31));
+    }
+}
+
+template <bool kSkin>
+__global__ void __launch_bounds__(kCurveThreads) curve_kernel(CurveArgs a) {
+    extern __shared__ __align__(16) float sm[];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int V = a.V;
+    const int cap = a.spb * V;
+    // shared layout (staged): x[3 cap] | arc[cap] | h[3 cap] | c[3 cap] | R[9 cap]
+    float* sx = sm;
+    float* sarc = a.staged ? sm + 3 * cap : sm;
+    float* sh = sm + 4 * cap;
+    float* sc = sm + 7 * cap;
+    float* sR = sm + 10 * cap;
+    const float inv_beta2 = __fdiv_rn(1.0f, __fmul_rn(a.beta, a.beta));
+    const float cutoff = __fmul_rn(3.0f, a.beta);
+
+    for (int g = blockIdx.x; g < a.ngroups; g += gridDim.x) {
+        const int64_t s0 = (int64_t)g * a.spb;
+        const int ns = (int)(a.N - s0 < a.spb ? a.N - s0 : a.spb);
+        const int P = ns * V;
+        const int64_t p0 = s0 * V;
+        const float* gx = a.x + 3 * p0;
+        if (a.staged) {
+            for (int k = tid; k < 3 * P; k += kCurveThreads) sx[k] = __ldg(gx + k);
+            if (kSkin) {
+                for (int k = tid; k < 3 * P; k += kCurveThreads) {
+                    sh[k] = __ldg(a.h + 3 * p0 + k);
+                    sc[k] = __ldg(a.c + 3 * p0 + k);
+                }
+                for (int k = tid; k < 9 * P; k += kCurveThreads) sR[k] = __ldg(a.R + 9 * p0 + k);
+            }
+        }
+        if (a.arc) {
+            for (int k = tid; k < P; k += kCurveThreads) sarc[k] = __ldg(a.arc + p0 + k);
+            __syncthreads();
+        } else {
+            __syncthreads();
+            const float* xs = a.staged ? sx : gx;
+            for (int s = warp; s < ns; s += kCurveThreads / 32) warp_arclength(xs + 3 * s * V, V, sarc + s * V, lane);
+            __syncthreads();
+        }
+        const float* X = a.staged ? sx : gx;
+        const float* Hh = a.staged ? sh : a.h + 3 * p0;
+        const float* Cc = a.staged ? sc : a.c + 3 * p0;
+        const float* RR = a.staged ? sR : a.R + 9 * p0;
+        for (int p = tid; p < P; p += kCurveThreads) {
+            const int sl = p / V;
+            const int i = p - sl * V;
+            const int b = sl * V;
+            const float si = sarc[p];
+            float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, sw = 0.f;
+            float xi0 = 0.f, xi1 = 0.f, xi2 = 0.f;
+            if (kSkin) { xi0 = X[3 * p]; xi1 = X[3 * p + 1]; xi2 = X[3 * p + 2]; }
+            for (int j = 0; j < V; ++j) {
+                const float dist = fabsf(__fsub_rn(si, sarc[b + j]));
+                if (dist > cutoff) continue;
+                const float w = expf(__fmul_rn(-__fmul_rn(dist, dist), inv_beta2));
+                const int q = b + j;
+                if (kSkin) {
+                    const float l0 = __fsub_rn(xi0, Hh[3 * q]);
+                    const float l1 = __fsub_rn(xi1, Hh[3 * q + 1]);
+                    const float l2 = __fsub_rn(xi2, Hh[3 * q + 2]);
+                    const float* r = RR + 9 * q;
+                    const float r0 = __fmaf_rn(r[2], l2, __fmaf_rn(r[1], l1, __fmul_rn(r[0], l0)));
+                    const float r1 = __fmaf_rn(r[5], l2, __fmaf_rn(r[4], l1, __fmul_rn(r[3], l0)));
+                    const float r2 = __fmaf_rn(r[8], l2, __fmaf_rn(r[7], l1, __fmul_rn(r[6], l0)));
+                    acc0 = __fmaf_rn(w, __fadd_rn(r0, Cc[3 * q]), acc0);
+                    acc1 = __fmaf_rn(w, __fadd_rn(r1, Cc[3 * q + 1]), acc1);
+                    acc2 = __fmaf_rn(w, __fadd_rn(r2, Cc[3 * q + 2]), acc2);
+                } else {
+                    acc0 = __fmaf_rn(w, X[3 * q], acc0);
+                    acc1 = __fmaf_rn(w, X[3 * q + 1], acc1);
+                    acc2 = __fmaf_rn(w, X[3 * q + 2], acc2);
+                }
+                sw = __fadd_rn(sw, w);
+            }
+            float* o = a.out + 3 * (p0 + p);
+            if (kSkin) {
+                const bool ok = sw > 1e-8f;
+                o[0] = ok ? __fdiv_rn(acc0, sw) : xi0;
+                o[1] = ok ? __fdiv_rn(acc1, sw) : xi1;
+                o[2] = ok ? __fdiv_rn(acc2, sw) : xi2;
+            } else {
+                const bool ok = sw > 1e-6f;
+                o[0] = ok ? __fdiv_rn(acc0, sw) : 0.f;
+                o[1] = ok ? __fdiv_rn(acc1, sw) : 0.f;
+                o[2] = ok ? __fdiv_rn(acc2, sw) : 0.f;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void arclength_kernel(int N, int V, const float* __restrict__ x, float* __restrict__ arc) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = w0; s < N; s += nw) warp_arclength(x + 3 * s * V, V, arc + s * V, lane);
+}
+
+s2c_status launch_curves(bool skin, int N, int V, const float* x, const float* arc, const float* h,
+                         const float* c, const float* R, float* out, float beta, cudaStream_t st) {
+    const char* name = skin ? "skinning" : "smooth_strands";
+    S2C_REQUIRE(N >= 0 && V >= 0, "%s: negative size (N=%d, V=%d)", name, N, V);
+    S2C_REQUIRE(N == 0 || V == 0 || (x && out), "%s: null strands or output", name);
+    S2C_REQUIRE(!skin || N == 0 || V == 0 || (h && c && R), "%s: null handle, canonical or rotation array", name);
+    if (N == 0 || V == 0) return S2C_OK;
+    const int bpp = skin ? kSkinBytes : kSmoothBytes;
+    CurveArgs a{};
+    a.N = N; a.V = V; a.x = x; a.arc = arc; a.h = h; a.c = c; a.R = R; a.out = out; a.beta = beta;
+    const int fit = kCurveSmem / bpp / V;       // whole strands a CTA can stage
+    size_t smem;
+    if (fit >= 1) {
+        // enough strands per CTA to fill its threads, few enough to give every SM work
+        const int want_threads = (kCurveThreads + V - 1) / V;
+        const int want_spread = (int)std::max<int64_t>(1, ((int64_t)N + 4 * num_sms() - 1) / (4 * num_sms()));
+        a.spb = std::min(fit, std::max(want_threads, std::min(want_spread, fit)));
+        a.staged = true;
+        smem = (size_t)a.spb * V * bpp;
+    } else {
+        S2C_REQUIRE(V <= kMaxArcOnly, "%s: strands of %d points exceed the staged limit of %d", name, V, kMaxArcOnly);
+        a.spb = 1;
+        a.staged = false;
+        smem = (size_t)V * 4;
+    }
+    a.ngroups = (int)(((int64_t)N + a.spb - 1) / a.spb);
+    const int blocks = (int)std::min<int64_t>(a.ngroups, (int64_t)num_sms() * 8);
+    if (skin)
+        curve_kernel<true><<<blocks, kCurveThreads, smem, st>>>(a);
+    else
+        curve_kernel<false><<<blocks, kCurveThreads, smem, st>>>(a);
+    S2C_CHECK_LAUNCH(name);
+    return S2C_OK;
+}
+
+}  // namespace
+}  // namespace s2c
+
+extern "C" {
+
+S2C_API s2c_status s2c_compute_arclength(int N, int V, const float* strands, float* arclength,
+                                         s2c_stream stream) {
+    S2C_REQUIRE(N >= 0 && V >= 0, "compute_arclength: negative size (N=%d, V=%d)", N, V);
+    if (N == 0 || V == 0) return S2C_OK;
+    S2C_REQUIRE(strands && arclength, "compute_arclength: null pointer");
+    const int threads = 256;
+    const unsigned blocks = s2c::grid_for((int64_t)N * 32, threads, (int64_t)s2c::num_sms() * 16);
+    s2c::arclength_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(N, V, strands, arclength);
+    S2C_CHECK_LAUNCH("compute_arclength");
+    return S2C_OK;
+}
+
+S2C_API s2c_status s2c_smooth_strands(int N, int V, const float* strands, const float* arclength,
+                                      float* smoothed_strands, float beta, s2c_stream stream) {
+    return s2c::launch_curves(false, N, V, strands, arclength, nullptr, nullptr, nullptr, smoothed_strands,
+                              beta, (cudaStream_t)stream);
+}
+
+S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float* arclength,
+                                const float* handle_strands, const float* canonical_handles,
+                                const float* R, float* skinned_strands, float beta, s2c_stream stream) {
+    return s2c::launch_curves(true, N, V, strands, arclength, handle_strands, canonical_handles, R,
+                              skinned_strands, beta, (cudaStream_t)stream);
+}
+
+}  // extern "C"

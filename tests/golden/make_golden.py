@@ -26,7 +26,7 @@ sys.path.insert(0, ROOT)
 
 from oracle.refkern import RefKernels  # noqa: E402
 from strns2cards_gb300 import synthetic as syn  # noqa: E402
-from strns2cards_gb300.mesh import build_edges_from_triangles  # noqa: E402
+from oracle.oracle import build_edges_from_triangles  # noqa: E402
 
 
 def sort_frags(pix: np.ndarray, attrs: np.ndarray):

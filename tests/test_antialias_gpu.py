@@ -2,8 +2,11 @@
 
 Silhouette decisions and normals are bit-identical to the reference.  The gradient d_pos
 is float: it must agree with the FP64 oracle (same FP32 decisions, FP64 window sums) to
-``|got - ref| <= 1e-5 * max(|ref|, 1e-3 * max|ref|)`` elementwise, and with the reference's
-own (FP32, __expf, atomics) gradient to the same bound.  Bit counts are exact.
+``|got - ref| <= 1e-5 * max(|ref|, 1e-3 * max|ref|)`` elementwise.  The reference's own
+gradient (FP32 chain rule, __expf, float atomics) is itself up to 7.3e-6 from FP64 in
+that norm on the golden case, so against it the bound is the sum of both, 2e-5.  The
+drop-in C entry with float atomics (as the reference) is held to the same 2e-5 against
+FP64.  Bit counts are exact.
 """
 import numpy as np
 import pytest
@@ -68,7 +71,28 @@ def test_antialias_gradient(tag, kr, rho):
     ok, err = grad_close(got, ora)
     assert ok, err
     assert np.array_equal(got != 0, ora != 0)
-    ok, err = grad_close(got, a["d_pos_" + tag])
+    ok, err = grad_close(got, a["d_pos_" + tag], tol=2e-5)
+    assert ok, err
+
+
+def test_antialias_float_atomic_entry():
+    """The reference-shaped C entry (no workspace, float atomics)."""
+    from strns2cards_gb300 import _core, _lib
+    import strns2cards_gb300 as s2c
+    a = golden("antialias.npz")
+    H, W = int(a["H"]), int(a["W"])
+    pos = cu(a["pos"])
+    ids, nrm = s2c.mark_discontinuity_edges((H, W), pos, cu(a["tri"]), cu(a["edges"]), cu(a["edge2tri"]))
+    fp, fa = s2c.dda_compute_fragments((H, W), pos, cu(a["edges"]), edge_ids=ids)
+    d_pos = torch.zeros_like(pos)
+    B, _, _, S = a["bitset"].shape
+    bits, tgt, e2c, ed = cu(a["bitset"]), cu(a["target"]), cu(a["edge2cluster"]), cu(a["edges"])
+    _lib.call("s2c_backward_antialiased_cluster_bitset", fp.shape[0], _lib.ptr(fp), _lib.ptr(fa), B, H, W, S,
+              _lib.ptr(bits), _lib.ptr(tgt), pos.shape[1], _lib.ptr(pos), ed.shape[0], _lib.ptr(ed),
+              _lib.ptr(nrm), _lib.ptr(e2c), _lib.ptr(d_pos), 7.0, 0.5, _lib.stream_of(pos))
+    ora = O.antialias_grad(a["bitset"], a["target"], a["pos"], a["tri"], a["edges"], a["edge2tri"], a["edge2cluster"],
+                           7.0, 0.5)
+    ok, err = grad_close(np_(d_pos), ora, tol=2e-5)
     assert ok, err
 
 

@@ -7,7 +7,7 @@ import numpy as np
 
 from conftest import GOLDEN
 from strns2cards_gb300 import synthetic as syn
-from strns2cards_gb300.mesh import build_edges_from_triangles
+from oracle.oracle import build_edges_from_triangles
 
 
 def sha(a):
