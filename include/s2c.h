@@ -280,6 +280,48 @@ S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float*
 S2C_API s2c_status s2c_build_edges_from_triangles(int T, const int32_t* tri, int32_t* edges,
                                                   int32_t* edge2tri, int64_t* num_edges);
 
+/* new: host.  CSR vertex adjacency of an undirected edge list (the uniform Laplacian's
+ * A of optimizer.py:70-99): neighbours of v in edge order, offsets (num_verts + 1),
+ * adj (2 E); *num_adj receives the count. */
+S2C_API s2c_status s2c_build_vertex_adjacency(int num_verts, int E, const int32_t* edges, int32_t* offsets,
+                                              int32_t* adj, int64_t* num_adj);
+
+/* ---------------------------------------------------------------------------------- *
+ * card deformation                                                                    *
+ * ---------------------------------------------------------------------------------- */
+
+/* new: Laplacian smoothing of card vertices, p <- p - lam * (p - mean of neighbours),
+ * `steps` Jacobi steps.  The reference has no kernel for it; it builds L = D - A of the
+ * card edges (optimizer.py:70-99) as preconditioner and regulariser (3_fitting.py:347-359).
+ * All cards share one topology: CSR adjacency (adj_offsets (verts_per_card + 1),
+ * adj (num_adj) local vertex ids); vertices (num_cards * verts_per_card, 3).  In place
+ * allowed.  A vertex without neighbours keeps its position. */
+S2C_API s2c_status s2c_card_laplacian_smooth(int num_cards, int verts_per_card, const int32_t* adj_offsets,
+                                             const int32_t* adj, int num_adj, const float* verts_in,
+                                             float* verts_out, float lam, int steps, s2c_stream stream);
+
+/* new: binding of strand vertices x (Nv, 3) to their 4 nearest guides (G, 3): idx (Nv, 4)
+ * (-1 where fewer than 4 guides exist), w (Nv, 4) = softmax(-d^2 / tau) over them, and the
+ * inverse lists (CSR over guides: list_offsets (G + 1), list_entries (4 Nv) = v * 4 + slot,
+ * ascending).  Distances are FP32 (dx^2 + dy^2) + dz^2; ties go to the lower guide index. */
+S2C_API size_t s2c_lbs_bind_workspace_size(int64_t num_verts, int num_guides);
+S2C_API s2c_status s2c_lbs_bind(int64_t num_verts, const float* x, int num_guides, const float* guides,
+                                float tau, int32_t* idx, float* w, int32_t* list_offsets,
+                                int32_t* list_entries, void* workspace, size_t workspace_bytes,
+                                s2c_stream stream);
+
+/* new: y = sum_k w_k (A_k x + t_k) with M (G, 3, 4) = [A | t] per guide. */
+S2C_API s2c_status s2c_lbs_forward(int64_t num_verts, const float* x, const int32_t* idx, const float* w,
+                                   int num_guides, const float* M, float* y, s2c_stream stream);
+
+/* new: gradients of the forward for grad_y (Nv, 3): grad_M (G, 3, 4) (overwritten; per-guide
+ * sums in the bind's list order) and, if non-NULL, grad_x (Nv, 3) = sum_k w_k A_k^T grad_y
+ * (weights held at their bound values).  Either output may be NULL. */
+S2C_API s2c_status s2c_lbs_backward(int64_t num_verts, const float* x, const int32_t* idx, const float* w,
+                                    int num_guides, const float* M, const int32_t* list_offsets,
+                                    const int32_t* list_entries, const float* grad_y, float* grad_M,
+                                    float* grad_x, s2c_stream stream);
+
 #ifdef __cplusplus
 }
 #endif

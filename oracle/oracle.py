@@ -47,6 +47,7 @@ _SIGS = {
     "or_accumulate_rgb": ([I64, I, i32p, f32p, f32p], None),
     "or_smooth_strands": ([I, I, f32p, f32p, f64p, F], None),
     "or_skinning": ([I, I, f32p, f32p, f32p, f32p, f32p, f64p, F], None),
+    "or_knn4": ([ctypes.c_int64, f32p, I, f32p, i32p, f32p], None),
 }
 
 # arithmetic-model flags (s2c_oracle.h)
@@ -350,3 +351,60 @@ def build_edges_from_triangles(tri: np.ndarray) -> Tuple[np.ndarray, np.ndarray]
     has2[has2] = ~first[nxt[has2]]
     e2t[has2, 1] = owner[nxt[has2]]
     return edges, e2t
+
+
+# ---- card Laplacian smoothing: p <- p - lam * D^-1 L p with the uniform Laplacian of
+# optimizer.py:70-99 (unique neighbour pairs, a self-loop counted once), FP64
+def card_laplacian_smooth(verts, quad_edges, verts_per_card, lam=0.5, steps=10):
+    nv = int(verts_per_card)
+    e = np.asarray(quad_edges, np.int64).reshape(-1, 2)
+    pairs = np.unique(np.concatenate([e, e[:, ::-1]], 0), axis=0) if e.size else np.zeros((0, 2), np.int64)
+    deg = np.bincount(pairs[:, 0], minlength=nv).astype(np.float64)
+    p = np.asarray(verts, np.float64).reshape(-1, nv, 3).copy()
+    has = deg > 0
+    for _ in range(int(steps)):
+        s = np.zeros_like(p)
+        np.add.at(s, (slice(None), pairs[:, 0]), p[:, pairs[:, 1]])
+        mean = s[:, has] / deg[has][None, :, None]
+        p[:, has] = p[:, has] - lam * (p[:, has] - mean)
+    return p.reshape(-1, 3)
+
+
+# ---- linear blend skinning to the 4 nearest guides: binding (exact FP32 selection, FP64
+# weights), forward and gradients in FP64
+def lbs_bind(x, guides, tau=0.01):
+    xs, g = _f32(np.asarray(x).reshape(-1, 3)), _f32(np.asarray(guides).reshape(-1, 3))
+    Nv, G = xs.shape[0], g.shape[0]
+    idx = np.empty((Nv, 4), np.int32)
+    d2 = np.empty((Nv, 4), np.float32)
+    lib().or_knn4(Nv, _p(xs, f32p), G, _p(g, f32p), _p(idx, ctypes.POINTER(ctypes.c_int32)), _p(d2, f32p))
+    ok = idx >= 0
+    d = d2.astype(np.float64)
+    e = np.where(ok, np.exp(-(np.where(ok, d, d[:, :1]) - d[:, :1]) / float(tau)), 0.0)
+    w = e / np.maximum(e.sum(1, keepdims=True), 1e-300)
+    return idx, w
+
+
+def lbs_forward(x, idx, w, M):
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    xh = np.concatenate([x, np.ones((x.shape[0], 1))], 1)
+    M = np.asarray(M, np.float64)
+    ok = idx >= 0
+    Mi = M[np.where(ok, idx, 0)]                               # (Nv, 4, 3, 4)
+    yk = np.einsum("vkrc,vc->vkr", Mi, xh)
+    return np.einsum("vk,vkr->vr", np.where(ok, w, 0.0), yk)
+
+
+def lbs_backward(x, idx, w, M, gy):
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    xh = np.concatenate([x, np.ones((x.shape[0], 1))], 1)
+    M = np.asarray(M, np.float64)
+    gy = np.asarray(gy, np.float64)
+    ok = idx >= 0
+    wz = np.where(ok, w, 0.0)
+    dM = np.zeros_like(M)
+    contrib = np.einsum("vk,vr,vc->vkrc", wz, gy, xh)
+    np.add.at(dM, np.where(ok, idx, 0).reshape(-1), contrib.reshape(-1, 3, 4) * ok.reshape(-1, 1, 1))
+    A = M[np.where(ok, idx, 0)][..., :3]                        # (Nv, 4, 3, 3)
+    dx = np.einsum("vk,vkrc,vr->vc", wz, A, gy)
+    return dM, dx

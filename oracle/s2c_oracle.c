@@ -678,3 +678,35 @@ void or_skinning(int N, int V, const float* strands, const float* arclength,
         }
     }
 }
+
+/* 4 nearest guides of each vertex by brute force, for the GPU binding of linear blend
+ * skinning: d^2 = (dx*dx + dy*dy) + dz*dz in FP32 (no contraction), ties to the lower
+ * guide index, non-finite distances never selected; idx = -1 / d2 = +inf where fewer
+ * than 4 guides qualify. */
+void or_knn4(int64_t Nv, const float* x, int G, const float* g, int32_t* idx, float* d2) {
+#pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < Nv; ++v) {
+        float bd[4] = {INFINITY, INFINITY, INFINITY, INFINITY};
+        int bi[4] = {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff};
+        const float qx = x[3 * v], qy = x[3 * v + 1], qz = x[3 * v + 2];
+        for (int i = 0; i < G; ++i) {
+            const float dx = qx - g[3 * i], dy = qy - g[3 * i + 1], dz = qz - g[3 * i + 2];
+            const float sx = dx * dx, sy = dy * dy, sz = dz * dz;
+            const float s = (sx + sy) + sz;
+            if (!(s < bd[3] || (s == bd[3] && i < bi[3]))) continue;
+            int k = 3;
+            while (k > 0 && (s < bd[k - 1] || (s == bd[k - 1] && i < bi[k - 1]))) {
+                bd[k] = bd[k - 1];
+                bi[k] = bi[k - 1];
+                --k;
+            }
+            bd[k] = s;
+            bi[k] = i;
+        }
+        for (int k = 0; k < 4; ++k) {
+            const int ok = bi[k] != 0x7fffffff && isfinite(bd[k]);
+            idx[4 * v + k] = ok ? bi[k] : -1;
+            d2[4 * v + k] = ok ? bd[k] : INFINITY;
+        }
+    }
+}

@@ -103,6 +103,7 @@ void or_smooth_strands(int N, int V, const float* strands, const float* arclengt
 void or_skinning(int N, int V, const float* strands, const float* arclength,
                  const float* handles, const float* canonical, const float* R,
                  double* out, float beta);
+void or_knn4(int64_t Nv, const float* x, int G, const float* g, int32_t* idx, float* d2);
 
 #ifdef __cplusplus
 }

@@ -62,6 +62,12 @@ SIGNATURES = {
     "s2c_smooth_strands": ([c_i, c_i, vp, vp, vp, c_f, vp], c_i),
     "s2c_skinning": ([c_i, c_i, vp, vp, vp, vp, vp, vp, c_f, vp], c_i),
     "s2c_build_edges_from_triangles": ([c_i, vp, vp, vp, i64p], c_i),
+    "s2c_build_vertex_adjacency": ([c_i, c_i, vp, vp, vp, i64p], c_i),
+    "s2c_card_laplacian_smooth": ([c_i, c_i, vp, vp, c_i, vp, vp, c_f, c_i, vp], c_i),
+    "s2c_lbs_bind_workspace_size": ([c_i64, c_i], c_sz),
+    "s2c_lbs_bind": ([c_i64, vp, c_i, vp, c_f, vp, vp, vp, vp, vp, c_sz, vp], c_i),
+    "s2c_lbs_forward": ([c_i64, vp, vp, vp, c_i, vp, vp, vp], c_i),
+    "s2c_lbs_backward": ([c_i64, vp, vp, vp, c_i, vp, vp, vp, vp, vp, vp, vp], c_i),
 }
 
 _lib = None

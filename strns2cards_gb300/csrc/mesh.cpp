@@ -52,3 +52,39 @@ extern "C" S2C_API s2c_status s2c_build_edges_from_triangles(int T, const int32_
     *num_edges = E;
     return S2C_OK;
 }
+
+// Vertex adjacency (CSR) of an undirected edge list, as the uniform Laplacian of
+// optimizer.py:70-99 sees it: neighbour pairs are unique (torch.unique over the pairs), a
+// self-loop (v, v) makes v its own neighbour once (it adds to the degree and cancels in
+// L p).  Neighbours of v are listed in the order of their first edge.  offsets has
+// num_verts + 1 entries, adj at most 2 * E; *num_adj receives the count written.
+extern "C" S2C_API s2c_status s2c_build_vertex_adjacency(int num_verts, int E, const int32_t* edges,
+                                                        int32_t* offsets, int32_t* adj, int64_t* num_adj) {
+    if (num_verts < 0 || E < 0 || !offsets || !num_adj || (E > 0 && (!edges || !adj))) {
+        s2c::set_error("build_vertex_adjacency: invalid arguments (V=%d, E=%d)", num_verts, E);
+        return S2C_ERR_INVALID;
+    }
+    std::vector<std::vector<int32_t>> nb((size_t)num_verts);
+    auto add = [&](int32_t a, int32_t b) {
+        for (int32_t u : nb[a])
+            if (u == b) return;
+        nb[a].push_back(b);
+    };
+    for (int e = 0; e < E; ++e) {
+        const int32_t a = edges[2 * e], b = edges[2 * e + 1];
+        if (a < 0 || a >= num_verts || b < 0 || b >= num_verts) {
+            s2c::set_error("build_vertex_adjacency: edge %d = (%d, %d) outside [0, %d)", e, a, b, num_verts);
+            return S2C_ERR_INVALID;
+        }
+        add(a, b);
+        if (b != a) add(b, a);
+    }
+    int64_t n = 0;
+    offsets[0] = 0;
+    for (int v = 0; v < num_verts; ++v) {
+        for (int32_t u : nb[v]) adj[n++] = u;
+        offsets[v + 1] = (int32_t)n;
+    }
+    *num_adj = n;
+    return S2C_OK;
+}
