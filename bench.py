@@ -293,6 +293,249 @@ def run_ours(args):
     return line
 
 
+# ---------------------------------------------------------------------------------------
+# Other rows of the path, each on its published configuration (``--workload NAME``).
+# A workload gives host inputs, an untimed setup on the device copies, a step, the units
+# one step processes and its algorithmic bytes; the harness below times it like the
+# headline (CUDA events per step, 256 MiB L2 flush between steps, clocks sampled) and
+# end to end (pinned host inputs copied in, result copied out, inside the timed region).
+# ---------------------------------------------------------------------------------------
+def _cards_scene(num_strands, num_verts, num_cards, quads_along, quads_across, res, seed=0):
+    from strns2cards_gb300 import synthetic as syn
+    strands = syn.make_strands(num_strands, num_verts, seed=seed)
+    mvp = syn.ortho_cameras(strands, margin=0.3, num_views=1)
+    cards = syn.make_cards(strands, 0, quads_along, quads_across, num_cards=num_cards)
+    return strands, mvp, cards
+
+
+def wl_tri_raster():
+    """Card raster of the 50,000 x 100 strand model: 2,048 cards (16 x 4 quads; 174,080 V,
+    262,144 T) -> rast (1, 1024, 1024, 4) and the cluster bitset (1, 1024, 1024, 64)."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    _, mvp, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
+    pos = syn.project(cards.verts, mvp)
+    host = {"pos": pos, "tri": cards.tri, "t2c": cards.tri2cluster}
+    V, T, H = pos.shape[1], cards.tri.shape[0], 1024
+
+    def step(d, st):
+        fp, fa = s2c.compute_fragments((H, H), d["pos"], d["tri"])
+        rast = s2c.depth_test(1, (H, H), fp, fa)
+        bits = s2c.cluster_mask_from_fragments((H, H), fp, fa, d["t2c"], 2048)
+        return rast, bits
+    return dict(name="tri_raster", host=host, step=step, units=T, unit="Mtri/s", scale=1e6,
+                metric="card triangles rasterised per second (rast + cluster bitset)",
+                alg_bytes=16 * V + 12 * T + 16 * H * H + 4 * H * H * 64, launches=None,
+                workload="2,048 cards (16x4 quads, 262,144 triangles) of the 50,000x100 strand model, 1024x1024, "
+                         "K=2048: compute_fragments + depth_test + cluster_mask_from_fragments")
+
+
+def wl_antialias():
+    """Antialias backward of the same cards against the strands' target bitset."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    strands, mvp, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
+    pos = syn.project(cards.verts, mvp)
+    spos = syn.project(strands.reshape(-1, 3), mvp)
+    sedges = syn.strand_edges(50_000, 100)
+    se2c = (np.arange(sedges.shape[0]) * 2048 // sedges.shape[0]).astype(np.int32)
+    edges, e2t = s2c.build_edges_from_triangles(cards.tri)
+    e2c = cards.tri2cluster[e2t[:, 0]].astype(np.int32)
+    host = {"pos": pos, "tri": cards.tri, "edges": edges, "e2t": e2t, "e2c": e2c}
+    V, E, H = pos.shape[1], edges.shape[0], 1024
+
+    def setup(d):
+        dev = d["pos"].device
+        tgt = s2c.dda_cluster_bitset((H, H), torch.from_numpy(spos).to(dev), torch.from_numpy(sedges).to(dev),
+                                     torch.from_numpy(se2c).to(dev), 2048)
+        fp, fa = s2c.compute_fragments((H, H), d["pos"], d["tri"])
+        bits = s2c.cluster_mask_from_fragments((H, H), fp, fa, torch.from_numpy(cards.tri2cluster).to(dev), 2048)
+        return {"tgt": tgt, "bits": bits}
+
+    def step(d, st):
+        return s2c.antialiased_cluster_bitset_grad(st["bits"], st["tgt"], d["pos"], d["tri"], d["edges"], d["e2t"],
+                                                   d["e2c"], 7.0, 0.5)
+    return dict(name="antialias", host=host, setup=setup, step=step, units=E, unit="Medge/s", scale=1e6,
+                metric="card edges through the antialiased bitset-loss backward per second",
+                alg_bytes=2 * 4 * H * H * 64 + 16 * V + 20 * E + 16 * V, launches=None,
+                workload="antialias backward (silhouette edges, edge DDA, 15x15 window, kernel_radius 7, rho 0.5) "
+                         "of 2,048 cards (434k edges) against the 50,000x100 strands' bitset, 1024x1024, K=2048")
+
+
+def wl_cluster_iou():
+    import torch
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(0)
+    H, S = 1024, 64
+    a = rng.integers(0, 2 ** 31 - 1, size=(1, H, H, S), dtype=np.int64).astype(np.int32)
+    b = a ^ (rng.random(a.shape) < 0.05).astype(np.int32)
+    host = {"a": a, "b": b}
+
+    def step(d, st):
+        return s2c.cluster_iou(d["a"], d["b"], 2048)[1:]
+    return dict(name="cluster_iou", host=host, step=step, units=2 * 4 * H * H * S, unit="GB/s", scale=1e9,
+                metric="per-card bitset IoU counts: bitset bytes read per second",
+                alg_bytes=2 * 4 * H * H * S, launches=1,
+                workload="per-card IoU counts of two int32 bitsets (1, 1024, 1024, 64), K=2048")
+
+
+def _strand_batch(N, V, seed=0):
+    from strns2cards_gb300 import synthetic as syn
+    return syn.make_strands(N, V, seed=seed).astype(np.float32)
+
+
+def wl_smooth_strands():
+    import strns2cards_gb300 as s2c
+    x = _strand_batch(100_000, 64)
+    host = {"x": x}
+
+    def step(d, st):
+        return s2c.smooth_strands(d["x"], 0.05)
+    n = x.shape[0] * x.shape[1]
+    return dict(name="smooth_strands", host=host, step=step, units=n, unit="Mpts/s", scale=1e6,
+                metric="strand points smoothed per second", alg_bytes=24 * n, launches=1,
+                workload="smooth_strands of 100,000 x 64 strands, beta 0.05 (arclength computed in the kernel)")
+
+
+def wl_skinning():
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(0)
+    x = _strand_batch(100_000, 64)
+    h = (x + rng.normal(scale=0.01, size=x.shape)).astype(np.float32)
+    c = (x + rng.normal(scale=0.02, size=x.shape)).astype(np.float32)
+    R = np.tile(np.eye(3, dtype=np.float32), (x.shape[0], x.shape[1], 1, 1))
+    host = {"x": x, "h": h, "c": c, "R": R}
+
+    def step(d, st):
+        return s2c.skinning(d["x"], d["h"], d["c"], d["R"], 0.05)
+    n = x.shape[0] * x.shape[1]
+    return dict(name="skinning", host=host, step=step, units=n, unit="Mpts/s", scale=1e6,
+                metric="strand points skinned per second", alg_bytes=(12 * 3 + 36 + 12) * n, launches=1,
+                workload="skinning of 100,000 x 64 strands to per-point handle frames, beta 0.05")
+
+
+def wl_lbs():
+    """Linear blend skinning of 100,000 x 64 strand vertices to the 4 nearest of 69,632 guides
+    (centre lines of 4,096 cards, 16 x 4 quads): forward + backward (dM and dx)."""
+    import torch
+    import strns2cards_gb300 as s2c
+    strands, _, cards = _cards_scene(100_000, 64, 4096, 16, 4, 2048)
+    x = strands.reshape(-1, 3).astype(np.float32)
+    g = np.ascontiguousarray(cards.verts.reshape(-1, 5, 17, 3)[:, 2].reshape(-1, 3), dtype=np.float32)
+    G = g.shape[0]
+    rng = np.random.default_rng(0)
+    M = (np.tile(np.eye(3, 4), (G, 1, 1)) + rng.normal(scale=0.05, size=(G, 3, 4))).astype(np.float32)
+    gy = torch.randn((x.shape[0], 3), generator=torch.Generator().manual_seed(0)).numpy()
+    host = {"x": x, "M": M, "gy": gy}
+
+    def setup(d):
+        return {"bind": s2c.LBSBinding(d["x"], torch.from_numpy(g).to(d["x"].device), 0.01)}
+
+    def step(d, st):
+        Mt = d["M"].requires_grad_(True)
+        xt = d["x"].requires_grad_(True)
+        y = s2c.lbs(xt, Mt, st["bind"])
+        dx, dM = torch.autograd.grad(y, (xt, Mt), d["gy"])
+        return y, dM, dx
+    Nv = x.shape[0]
+    fwd = 12 * Nv + 32 * Nv + 48 * G + 12 * Nv
+    bwd = 12 * Nv + 32 * Nv + 12 * Nv + 48 * G + 16 * Nv + 12 * Nv + 16 * Nv   # dx pass + dM pass
+    return dict(name="lbs", host=host, setup=setup, step=step, units=Nv, unit="Mverts/s", scale=1e6,
+                metric="strand vertices through LBS forward + backward per second", alg_bytes=fwd + bwd, launches=3,
+                workload="LBS of 100,000 x 64 strand vertices to 4 nearest of 69,632 guides (4,096 cards): "
+                         "forward, backward dM (per-guide lists) and dx")
+
+
+def wl_laplacian():
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    _, _, h, w = syn.grid_strip(5, 33)
+    qe = np.concatenate([h, w], 0)
+    nv, cards = 165, 4096
+    p = np.random.default_rng(0).normal(size=(cards * nv, 3)).astype(np.float32)
+    host = {"p": p}
+
+    def setup(d):
+        return {"lap": s2c.CardLaplacian(nv, qe, d["p"].device)}
+
+    def step(d, st):
+        return st["lap"](d["p"], 0.5, 10)
+    return dict(name="laplacian", host=host, setup=setup, step=step, units=cards * nv * 10, unit="Mvert-steps/s",
+                scale=1e6, metric="card vertex Jacobi steps per second", alg_bytes=24 * cards * nv, launches=1,
+                workload="10 Jacobi Laplacian steps (lambda 0.5) on 4,096 cards of 32x4 quads (165 vertices each)")
+
+
+WORKLOADS = {"tri_raster": wl_tri_raster, "antialias": wl_antialias, "cluster_iou": wl_cluster_iou,
+             "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
+             "laplacian": wl_laplacian}
+
+
+def run_workload(args):
+    import torch
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        print(json.dumps({"workload": args.workload, "skipped": "secondary workloads run on one GPU"}))
+        return
+    dev = torch.device("cuda", 0)
+    wl = WORKLOADS[args.workload]()
+    d = {k: torch.from_numpy(np.ascontiguousarray(v)).to(dev) for k, v in wl["host"].items()}
+    st = wl["setup"](d) if "setup" in wl else None
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(args.warmup, 3)):
+        wl["step"](d, st)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.fill_(i & 0xff)
+            evs[i][0].record(stream)
+            wl["step"](d, st)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    t = sum(ms) / 1e3
+    value = wl["units"] * args.steps / t / wl["scale"]
+    # end to end: pinned host inputs in, every output tensor back
+    pinned = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in wl["host"].items()}
+    h2d = sum(v.nbytes for v in wl["host"].values())
+
+    def outs(r):
+        return [x for x in (r if isinstance(r, (tuple, list)) else (r,)) if isinstance(x, torch.Tensor)]
+    probe = outs(wl["step"](d, st))
+    host_out = [torch.empty(x.shape, dtype=x.dtype).pin_memory() for x in probe]
+    d2h = sum(x.numel() * x.element_size() for x in probe)
+
+    def e2e_step():
+        dd = {k: v.to(dev, non_blocking=True) for k, v in pinned.items()}
+        for ho, x in zip(host_out, outs(wl["step"](dd, st))):
+            ho.copy_(x, non_blocking=True)
+    e2e_step()
+    torch.cuda.synchronize()
+    ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k = max(3, min(args.steps, 10))
+    ea.record(stream)
+    for _ in range(k):
+        e2e_step()
+    eb.record(stream)
+    torch.cuda.synchronize()
+    e2e = wl["units"] * k / (ea.elapsed_time(eb) / 1e3) / wl["scale"]
+    peak, peak_kind = load_peaks()
+    achieved = wl["alg_bytes"] / (t / args.steps) / 1e9
+    line = {"metric": wl["metric"], "value": value, "unit": wl["unit"], "n_gpus": 1, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": wl["workload"], "l2": "flushed between steps (256 MiB write)"},
+            "e2e": {"value": e2e, "unit": wl["unit"], "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "algorithmic_bytes_per_step": wl["alg_bytes"], "traffic": None},
+            "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": None, "step_ms": ms}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,9 +543,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["dda_bitset"] + sorted(WORKLOADS), default="dda_bitset",
+                    help="dda_bitset (default) is the headline; the others time the remaining rows")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "dda_bitset":
+        run_workload(args)
     else:
         run_ours(args)
 

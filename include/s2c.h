@@ -148,6 +148,13 @@ S2C_API s2c_status s2c_depth_test(int B, int H, int W, int64_t num_frags, const 
                                   const float* frag_attrs, float* rast_out, void* workspace,
                                   size_t workspace_bytes, s2c_stream stream);
 
+/* new: d(b0, b1)/d(x, y) in pixel units, rast_db (B, H, W, 4) = (db0/dx, db0/dy, db1/dx,
+ * db1/dy), from the clip-space edge functions of the forward (rasterize.cu:144-156) for the
+ * triangle id in rast (B, H, W, 4); 0 where rast is empty.  The reference has no such output. */
+S2C_API s2c_status s2c_barycentric_derivatives(int B, int H, int W, int V, const float* pos, int T,
+                                               const int32_t* tri, const float* rast, float* rast_db,
+                                               s2c_stream stream);
+
 /* replaces: interpolate_triangle_attributes (pystrns2cards.cpp:394-415; rasterize.cu:367-455).
  * image (B, H, W, C) pre-zeroed by the caller. */
 S2C_API s2c_status s2c_interpolate_triangle_attributes(int B, int H, int W, int C, const float* rast,

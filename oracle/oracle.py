@@ -408,3 +408,31 @@ def lbs_backward(x, idx, w, M, gy):
     A = M[np.where(ok, idx, 0)][..., :3]                        # (Nv, 4, 3, 3)
     dx = np.einsum("vk,vkrc,vr->vc", wz, A, gy)
     return dM, dx
+
+
+# ---- barycentric derivatives (new output): the forward's clip-space edge functions
+# (rasterize.cu:144-156) at the pixel centre, differentiated in FP64
+def barycentric_derivatives(rast, pos, tri):
+    rast = np.asarray(rast, np.float32)
+    B, H, W, _ = rast.shape
+    out = np.zeros((B, H, W, 4), np.float64)
+    t = rast[..., 3].astype(np.int64) - 1
+    b, y, x = np.nonzero(t >= 0)
+    tt = t[b, y, x]
+    # pixel centre in NDC, in FP32 as the forward computes it
+    px = (np.float32(-1) + (np.float32(2) * (x.astype(np.float32) + np.float32(0.5))) / np.float32(W)).astype(np.float64)
+    py = (np.float32(-1) + (np.float32(2) * (y.astype(np.float32) + np.float32(0.5))) / np.float32(H)).astype(np.float64)
+    P = np.asarray(pos, np.float64)[b[:, None], np.asarray(tri)[tt]]          # (n, 3, 4)
+    qx = P[..., 0] - px[:, None] * P[..., 3]
+    qy = -P[..., 1] - py[:, None] * P[..., 3]
+    j, k = [1, 2, 0], [2, 0, 1]
+    A = qx[:, j] * qy[:, k] - qy[:, j] * qx[:, k]                               # (n, 3)
+    dAx = P[:, j, 3] * P[:, k, 1] - P[:, k, 3] * P[:, j, 1]
+    dAy = P[:, j, 3] * P[:, k, 0] - P[:, k, 3] * P[:, j, 0]
+    S = A.sum(1)
+    ok = S != 0
+    bb = A / np.where(ok, S, 1.0)[:, None]
+    for i in range(2):
+        out[b, y, x, 2 * i] = np.where(ok, (dAx[:, i] - bb[:, i] * dAx.sum(1)) / np.where(ok, S, 1.0) * (2.0 / W), 0.0)
+        out[b, y, x, 2 * i + 1] = np.where(ok, (dAy[:, i] - bb[:, i] * dAy.sum(1)) / np.where(ok, S, 1.0) * (2.0 / H), 0.0)
+    return out

@@ -228,9 +228,84 @@ __global__ void __launch_bounds__(256) dda_interp_backward_kernel(int64_t npix, 
     }
 }
 
+// Barycentric derivatives (no counterpart in the reference, whose rasteriser outputs
+// barycentrics only): d(b0, b1)/d(x, y) in pixel units at every covered pixel of rast.
+// The forward's clip-space edge functions (rasterize.cu:144-156) A_i = q_j x q_k with
+// q_j = (x_j - px w_j, -y_j - py w_j) are affine in (px, py):
+// dA_i/dpx = w_j y_k - w_k y_j and dA_i/dpy = w_j x_k - w_k x_j for (i, j, k) cyclic, so
+// db_i/dpx = (dA_i/dpx - b_i sum_m dA_m/dpx) / A, with dpx/dx = 2 / W and dpy/dy = 2 / H.
+// Output (du/dx, du/dy, dv/dx, dv/dy) for (u, v) = (b0, b1); 0 where the pixel is empty.
+__global__ void __launch_bounds__(256) bary_db_kernel(int B, int H, int W, Tris R, const float4* __restrict__ rast,
+                                                      float4* __restrict__ db) {
+    const int64_t n = (int64_t)B * H * W;
+    const float sxp = __fdiv_rn(2.f, (float)W), syp = __fdiv_rn(2.f, (float)H);
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (int64_t)gridDim.x * blockDim.x) {
+        const float4 r = __ldg(rast + idx);
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int t = f2i(r.w) - 1;
+        const int64_t bh = idx / W;
+        const int x = (int)(idx - bh * W);
+        const int b = (int)(bh / H);
+        const int y = (int)(bh - (int64_t)b * H);
+        if (t >= 0 && t < R.T) {
+            const int i0 = __ldg(R.tri + 3 * t), i1 = __ldg(R.tri + 3 * t + 1), i2 = __ldg(R.tri + 3 * t + 2);
+            if ((unsigned)i0 < (unsigned)R.V && (unsigned)i1 < (unsigned)R.V && (unsigned)i2 < (unsigned)R.V) {
+                const float4* pb = R.pos4 + (int64_t)b * R.V;
+                const float4 P0 = __ldg(pb + i0), P1 = __ldg(pb + i1), P2 = __ldg(pb + i2);
+                const float px = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)x, 0.5f)), (float)W));
+                const float py = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)y, 0.5f)), (float)H));
+                const float q0x = __fmaf_rn(-px, P0.w, P0.x), q0y = __fmaf_rn(-py, P0.w, -P0.y);
+                const float q1x = __fmaf_rn(-px, P1.w, P1.x), q1y = __fmaf_rn(-py, P1.w, -P1.y);
+                const float q2x = __fmaf_rn(-px, P2.w, P2.x), q2y = __fmaf_rn(-py, P2.w, -P2.y);
+                const float A0 = __fmaf_rn(q1x, q2y, -__fmul_rn(q1y, q2x));
+                const float A1 = __fmaf_rn(q2x, q0y, -__fmul_rn(q2y, q0x));
+                const float A2 = __fmaf_rn(q0x, q1y, -__fmul_rn(q0y, q1x));
+                const float A = __fadd_rn(__fadd_rn(A0, A1), A2);
+                if (A != 0.f) {
+                    const float a0x = __fmaf_rn(P1.w, P2.y, -__fmul_rn(P2.w, P1.y));
+                    const float a1x = __fmaf_rn(P2.w, P0.y, -__fmul_rn(P0.w, P2.y));
+                    const float a2x = __fmaf_rn(P0.w, P1.y, -__fmul_rn(P1.w, P0.y));
+                    const float a0y = __fmaf_rn(P1.w, P2.x, -__fmul_rn(P2.w, P1.x));
+                    const float a1y = __fmaf_rn(P2.w, P0.x, -__fmul_rn(P0.w, P2.x));
+                    const float a2y = __fmaf_rn(P0.w, P1.x, -__fmul_rn(P1.w, P0.x));
+                    const float sx = __fadd_rn(__fadd_rn(a0x, a1x), a2x);
+                    const float sy = __fadd_rn(__fadd_rn(a0y, a1y), a2y);
+                    const float b0 = r.x, b1 = r.y;
+                    o.x = __fmul_rn(__fdiv_rn(__fmaf_rn(-b0, sx, a0x), A), sxp);
+                    o.y = __fmul_rn(__fdiv_rn(__fmaf_rn(-b0, sy, a0y), A), syp);
+                    o.z = __fmul_rn(__fdiv_rn(__fmaf_rn(-b1, sx, a1x), A), sxp);
+                    o.w = __fmul_rn(__fdiv_rn(__fmaf_rn(-b1, sy, a1y), A), syp);
+                }
+            }
+        }
+        db[idx] = o;
+    }
+}
+
 }  // namespace s2c
 
 using namespace s2c;
+
+extern "C" s2c_status s2c_barycentric_derivatives(int B, int H, int W, int V, const float* pos, int T,
+                                                  const int32_t* tri, const float* rast, float* rast_db,
+                                                  s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && V >= 0 && T >= 0, "barycentric_derivatives: bad sizes");
+    const int64_t n = (int64_t)B * H * W;
+    if (n == 0) return S2C_OK;
+    S2C_REQUIRE(rast && rast_db && (V == 0 || pos) && (T == 0 || tri), "barycentric_derivatives: null pointer");
+    S2C_REQUIRE(((uintptr_t)rast & 15) == 0 && ((uintptr_t)rast_db & 15) == 0 && ((uintptr_t)pos & 15) == 0,
+                "barycentric_derivatives: misaligned");
+    Tris R;
+    R.pos4 = (const float4*)pos;
+    R.tri = tri;
+    R.V = V;
+    R.T = T;
+    R.divT = FastDiv((uint32_t)(T > 0 ? T : 1));
+    bary_db_kernel<<<grid_for(n, 256, (int64_t)num_sms() * 16), 256, 0, (cudaStream_t)stream>>>(
+        B, H, W, R, (const float4*)rast, (float4*)rast_db);
+    S2C_CHECK_LAUNCH("bary_db_kernel");
+    return S2C_OK;
+}
 
 static Tris make_tris(int V, const float* pos, int T, const int32_t* tri) {
     Tris R;

@@ -5,7 +5,7 @@ from typing import Optional, Tuple
 
 import torch
 
-from . import _core
+from . import _core, _lib
 
 
 def compute_fragments(
@@ -66,6 +66,31 @@ def rasterize(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.Tensor)
     """``compute_fragments`` then ``depth_test`` (``rasterize.py:97-116``)."""
     frag_pix, frag_attrs = compute_fragments(resolution, pos, tri)
     return depth_test(pos.shape[0], resolution, frag_pix, frag_attrs)
+
+
+def barycentric_derivatives(rast: torch.Tensor, pos: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:
+    """d(b0, b1)/d(x, y) in pixel units, (B, H, W, 4) = (db0/dx, db0/dy, db1/dx, db1/dy), of the
+    triangle covering each pixel of ``rast``; zeros where empty.  Not in the reference."""
+    if not (rast.is_cuda and pos.is_cuda and tri.is_cuda):
+        raise ValueError("All inputs must be CUDA tensors.")
+    if rast.ndim != 4 or rast.shape[-1] != 4 or pos.ndim != 3 or pos.shape[-1] != 4 or tri.ndim != 2:
+        raise ValueError("rast must be (B, H, W, 4), pos (B, V, 4) and tri (T, 3).")
+    if rast.shape[0] > pos.shape[0]:
+        raise ValueError("pos must hold every view of rast.")
+    r = rast.contiguous()
+    db = torch.empty_like(r)
+    B, H, W, _ = r.shape
+    p = pos.contiguous()
+    t = tri.contiguous()
+    _lib.call("s2c_barycentric_derivatives", B, H, W, p.shape[1], _lib.ptr(p), t.shape[0], _lib.ptr(t), _lib.ptr(r),
+              _lib.ptr(db), _lib.stream_of(r))
+    return db
+
+
+def rasterize_with_derivatives(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.Tensor):
+    """``rasterize`` plus ``barycentric_derivatives``: (rast, rast_db)."""
+    rast = rasterize(resolution, pos, tri)
+    return rast, barycentric_derivatives(rast, pos, tri)
 
 
 class InterpolateTriangleAttributes(torch.autograd.Function):

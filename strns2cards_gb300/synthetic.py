@@ -171,10 +171,17 @@ class Cards:
 
 
 def make_cards(strands: np.ndarray, per_cluster: int, quads_along: int, quads_across: int,
-               width_scale: float = 2.0) -> Cards:
-    """One grid strip per cluster that follows the cluster's mean strand."""
+               width_scale: float = 2.0, num_cards: int = 0) -> Cards:
+    """One grid strip per cluster that follows the cluster's mean strand.  Clusters are
+    runs of ``per_cluster`` consecutive strands, or, with ``num_cards`` > 0, the balanced
+    split strand k -> card k * num_cards // N."""
     N, V, _ = strands.shape
-    K = (N + per_cluster - 1) // per_cluster
+    if num_cards > 0:
+        K = int(num_cards)
+        starts = (np.arange(K + 1) * N + K - 1) // K              # first strand s with s*K//N == k
+    else:
+        K = (N + per_cluster - 1) // per_cluster
+        starts = np.minimum(np.arange(K + 1) * per_cluster, N)
     cols = quads_along + 1
     rows = quads_across + 1
     faces, quads, h_e, w_e = grid_strip(rows, cols)
@@ -185,7 +192,7 @@ def make_cards(strands: np.ndarray, per_cluster: int, quads_along: int, quads_ac
     hi = np.minimum(lo + 1, V - 1)
     fr = (src - lo)[:, None]
     for k in range(K):
-        cl = strands[k * per_cluster:(k + 1) * per_cluster].astype(np.float64)
+        cl = strands[starts[k]:starts[k + 1]].astype(np.float64)
         mean = cl.mean(0)
         centre = (1.0 - fr) * mean[lo] + fr * mean[hi]           # (cols, 3)
         tangent = mean[-1] - mean[0]

@@ -156,3 +156,37 @@ def test_depth_test_of_line_fragments():
     ties = tie_pixels(ofp, ofa, B, H, W)
     assert np.array_equal(rast[~ties], ref[~ties])
     assert np.array_equal(rast[ties][:, 2], ref[ties][:, 2])  # same depth at the ties
+
+
+@pytest.mark.parametrize("name", ["tri_cards", "tri_random"])
+def test_barycentric_derivatives(name):
+    """db/dxy against the FP64 oracle (max-norm 1e-5), and against a central difference of
+    the reference's own barycentrics across neighbouring pixels of the same triangle."""
+    import strns2cards_gb300 as s2c
+    d = golden(name + ".npz")
+    H, W = int(d["H"]), int(d["W"])
+    rast, db = s2c.rasterize_with_derivatives((H, W), cu(d["pos"]), cu(d["tri"]))
+    got = np_(db)
+    ref = O.barycentric_derivatives(np_(rast), d["pos"], d["tri"])
+    assert close(got, ref)
+    assert np.array_equal(np.any(got != 0, -1), np.any(ref != 0, -1) | np.any(got != 0, -1))
+    # b is affine in NDC for orthographic views (w = 1): the golden barycentrics one pixel
+    # apart differ by exactly db/dx
+    r = d["rast"]
+    if np.allclose(d["pos"][..., 3], 1.0):
+        same = (r[:, :, 1:, 3] == r[:, :, :-1, 3]) & (r[:, :, 1:, 3] > 0)
+        fd = (r[:, :, 1:, 0] - r[:, :, :-1, 0]).astype(np.float64)
+        an = ref[:, :, :-1, 0]
+        assert np.abs(fd[same] - an[same]).max() <= 1e-3 * max(np.abs(an[same]).max(), 1e-6)
+
+
+def test_barycentric_derivatives_perspective():
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(22)
+    V, T, B = 300, 200, 2
+    pos = rng.uniform(-1.2, 1.2, size=(B, V, 4)).astype(np.float32)
+    pos[..., 3] = rng.uniform(0.5, 1.5, size=(B, V))
+    pos[..., 2] *= pos[..., 3] * 0.7
+    tri = rng.integers(0, V, size=(T, 3)).astype(np.int32)
+    rast, db = s2c.rasterize_with_derivatives((70, 90), cu(pos), cu(tri))
+    assert close(np_(db), O.barycentric_derivatives(np_(rast), pos, tri))
