@@ -308,7 +308,7 @@ def _cards_scene(num_strands, num_verts, num_cards, quads_along, quads_across, r
     return strands, mvp, cards
 
 
-def wl_tri_raster():
+def wl_tri_raster(list_path=False):
     """Card raster of the 50,000 x 100 strand model: 2,048 cards (16 x 4 quads; 174,080 V,
     262,144 T) -> rast (1, 1024, 1024, 4) and the cluster bitset (1, 1024, 1024, 64)."""
     import torch
@@ -319,19 +319,29 @@ def wl_tri_raster():
     host = {"pos": pos, "tri": cards.tri, "t2c": cards.tri2cluster}
     V, T, H = pos.shape[1], cards.tri.shape[0], 1024
 
+    def setup(d):
+        return {"ws": torch.empty(8 * H * H + 256, dtype=torch.uint8, device=d["pos"].device),
+                "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=d["pos"].device),
+                "bits": torch.empty((1, H, H, 64), dtype=torch.int32, device=d["pos"].device)}
+
     def step(d, st):
-        fp, fa = s2c.compute_fragments((H, H), d["pos"], d["tri"])
-        rast = s2c.depth_test(1, (H, H), fp, fa)
-        bits = s2c.cluster_mask_from_fragments((H, H), fp, fa, d["t2c"], 2048)
-        return rast, bits
-    return dict(name="tri_raster", host=host, step=step, units=T, unit="Mtri/s", scale=1e6,
+        if list_path:
+            fp, fa = s2c.compute_fragments((H, H), d["pos"], d["tri"])
+            rast = s2c.depth_test(1, (H, H), fp, fa)
+            bits = s2c.cluster_mask_from_fragments((H, H), fp, fa, d["t2c"], 2048)
+            return rast, bits
+        return s2c.rasterize_fused((H, H), d["pos"], d["tri"], d["t2c"], 2048, rast=st["rast"], bitset=st["bits"],
+                                   workspace=st["ws"])
+    how = ("compute_fragments + depth_test + cluster_mask_from_fragments (the reference's op sequence)"
+           if list_path else "one fused pass (rasterize_fused)")
+    return dict(name="tri_raster", host=host, setup=setup, step=step, units=T, unit="Mtri/s", scale=1e6,
                 metric="card triangles rasterised per second (rast + cluster bitset)",
-                alg_bytes=16 * V + 12 * T + 16 * H * H + 4 * H * H * 64, launches=None,
+                alg_bytes=16 * V + 12 * T + 16 * H * H + 4 * H * H * 64, launches=None if list_path else 3,
                 workload="2,048 cards (16x4 quads, 262,144 triangles) of the 50,000x100 strand model, 1024x1024, "
-                         "K=2048: compute_fragments + depth_test + cluster_mask_from_fragments")
+                         "K=2048: " + how)
 
 
-def wl_antialias():
+def wl_antialias(list_path=False):
     """Antialias backward of the same cards against the strands' target bitset."""
     import torch
     import strns2cards_gb300 as s2c
@@ -356,12 +366,55 @@ def wl_antialias():
 
     def step(d, st):
         return s2c.antialiased_cluster_bitset_grad(st["bits"], st["tgt"], d["pos"], d["tri"], d["edges"], d["e2t"],
-                                                   d["e2c"], 7.0, 0.5)
+                                                   d["e2c"], 7.0, 0.5, fused=not list_path)
+    how = ("mark_discontinuity_edges + dda_compute_fragments + backward (the reference's op sequence)"
+           if list_path else "one fused pass per (view, edge)")
     return dict(name="antialias", host=host, setup=setup, step=step, units=E, unit="Medge/s", scale=1e6,
                 metric="card edges through the antialiased bitset-loss backward per second",
-                alg_bytes=2 * 4 * H * H * 64 + 16 * V + 20 * E + 16 * V, launches=None,
+                alg_bytes=2 * 4 * H * H * 64 + 16 * V + 20 * E + 16 * V, launches=None if list_path else 2,
                 workload="antialias backward (silhouette edges, edge DDA, 15x15 window, kernel_radius 7, rho 0.5) "
-                         "of 2,048 cards (434k edges) against the 50,000x100 strands' bitset, 1024x1024, K=2048")
+                         "of 2,048 cards (434k edges) against the 50,000x100 strands' bitset, 1024x1024, K=2048: "
+                         + how)
+
+
+def wl_iteration():
+    """One plain fit iteration of the 50,000 x 100 model: card raster (rast + bitset),
+    antialias forward (XOR loss) and backward, per-card IoU."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    strands, mvp, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
+    pos = syn.project(cards.verts, mvp)
+    spos = syn.project(strands.reshape(-1, 3), mvp)
+    sedges = syn.strand_edges(50_000, 100)
+    se2c = (np.arange(sedges.shape[0]) * 2048 // sedges.shape[0]).astype(np.int32)
+    edges, e2t = s2c.build_edges_from_triangles(cards.tri)
+    e2c = cards.tri2cluster[e2t[:, 0]].astype(np.int32)
+    host = {"pos": pos, "tri": cards.tri, "t2c": cards.tri2cluster, "edges": edges, "e2t": e2t, "e2c": e2c}
+    V, T, E, H = pos.shape[1], cards.tri.shape[0], edges.shape[0], 1024
+
+    def setup(d):
+        dev = d["pos"].device
+        tgt = s2c.dda_cluster_bitset((H, H), torch.from_numpy(spos).to(dev), torch.from_numpy(sedges).to(dev),
+                                     torch.from_numpy(se2c).to(dev), 2048)
+        return {"tgt": tgt, "ws": torch.empty(8 * H * H + 256, dtype=torch.uint8, device=dev),
+                "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=dev),
+                "bits": torch.empty((1, H, H, 64), dtype=torch.int32, device=dev)}
+
+    def step(d, st):
+        rast, bits = s2c.rasterize_fused((H, H), d["pos"], d["tri"], d["t2c"], 2048, rast=st["rast"],
+                                         bitset=st["bits"], workspace=st["ws"])
+        loss = s2c.xor_error(bits, st["tgt"])
+        d_pos = s2c.antialiased_cluster_bitset_grad(bits, st["tgt"], d["pos"], d["tri"], d["edges"], d["e2t"],
+                                                    d["e2c"], 7.0, 0.5)
+        iou = s2c.cluster_iou(bits, st["tgt"], 2048)[1:]
+        return (rast, loss, d_pos) + tuple(iou)
+    alg = (16 * V + 12 * T + 16 * H * H + 4 * H * H * 64) + 2 * 4 * H * H * 64 + \
+          (2 * 4 * H * H * 64 + 16 * V + 20 * E + 16 * V) + 2 * 4 * H * H * 64
+    return dict(name="iteration", host=host, setup=setup, step=step, units=1, unit="iter/s", scale=1.0,
+                metric="plain fit iterations per second", alg_bytes=alg, launches=None,
+                workload="one fit iteration of 2,048 cards against the 50,000x100 strands' bitset, 1024x1024, "
+                         "K=2048: fused raster (rast + bitset), XOR loss, fused antialias backward, per-card IoU")
 
 
 def wl_cluster_iou():
@@ -467,7 +520,9 @@ def wl_laplacian():
                 workload="10 Jacobi Laplacian steps (lambda 0.5) on 4,096 cards of 32x4 quads (165 vertices each)")
 
 
-WORKLOADS = {"tri_raster": wl_tri_raster, "antialias": wl_antialias, "cluster_iou": wl_cluster_iou,
+WORKLOADS = {"tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
+             "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
+             "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
              "laplacian": wl_laplacian}
 

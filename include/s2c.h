@@ -148,6 +148,17 @@ S2C_API s2c_status s2c_depth_test(int B, int H, int W, int64_t num_frags, const 
                                   const float* frag_attrs, float* rast_out, void* workspace,
                                   size_t workspace_bytes, s2c_stream stream);
 
+/* new: compute_fragments + depth_test + cluster_mask_from_fragments in one pass without a
+ * fragment list or host synchronisation (capturable in a CUDA graph).  rast (B, H, W, 4)
+ * (nullable) equals depth_test's output (exact depth ties go to the lower triangle id);
+ * bitset (B, H, W, S) (nullable; zeroed here) equals cluster_mask_from_fragments' for
+ * tri2cluster (num_tri2cluster entries).  The workspace holds B*H*W 64-bit depth keys
+ * (needed only with rast). */
+S2C_API size_t s2c_rasterize_fused_workspace_size(int B, int H, int W);
+S2C_API s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
+                                       const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
+                                       float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream);
+
 /* new: d(b0, b1)/d(x, y) in pixel units, rast_db (B, H, W, 4) = (db0/dx, db0/dy, db1/dx,
  * db1/dy), from the clip-space edge functions of the forward (rasterize.cu:144-156) for the
  * triangle id in rast (B, H, W, 4); 0 where rast is empty.  The reference has no such output. */
@@ -247,6 +258,17 @@ S2C_API s2c_status s2c_backward_antialiased_cluster_bitset_f64(
     const int32_t* bitset, const int32_t* target, int V, const float* pos, int E,
     const int32_t* edges, const float* normals, const int32_t* edge2cluster, float* d_pos,
     float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream);
+
+/* new: the whole gradient of antialias.py:100-122 in one pass -- the silhouette test, the
+ * DDA walk of each marked edge and every fragment's window, fused per (view, edge), with no
+ * fragment list and no host synchronisation (capturable in a CUDA graph).  Same
+ * contributions as mark_discontinuity_edges + dda_compute_fragments + the backward above;
+ * d_pos (B, V, 4) accumulated via the FP64 workspace (B*V*3 doubles). */
+S2C_API size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V);
+S2C_API s2c_status s2c_antialiased_cluster_bitset_grad(
+    int B, int H, int W, int S, const int32_t* bitset, const int32_t* target, int V, const float* pos, int T,
+    const int32_t* tri, int E, const int32_t* edges, const int32_t* edge2tri, const int32_t* edge2cluster,
+    float* d_pos, float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream);
 
 /* ---------------------------------------------------------------------------------- *
  * strand curves                                                                       *

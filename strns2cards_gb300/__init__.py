@@ -13,5 +13,5 @@ from .dda import (DDAInterpolateAttributes, dda_cluster_bitset, dda_compute_frag
 from .mesh import build_edges_from_triangles  # noqa: F401
 from .rasterize import (InterpolateTriangleAttributes, barycentric_derivatives, cluster_mask_from_fragments,  # noqa: F401
                         compute_fragments, depth_test, interpolate_triangle_attributes, rasterize,
-                        rasterize_with_derivatives)
+                        rasterize_fused, rasterize_with_derivatives)
 from . import _core  # noqa: F401

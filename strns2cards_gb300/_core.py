@@ -312,6 +312,35 @@ def backward_antialiased_cluster_bitset(frag_pix, frag_attrs_dda, bitset, target
          float(kernel_radius), float(rho), ptr(ws), ws.numel(), _stream(pos))
 
 
+def antialiased_cluster_bitset_grad(bitset, target_bitset, pos, tri, edges, edge2tri, edge2cluster, kernel_radius,
+                                    rho, d_pos=None, ws=None) -> torch.Tensor:
+    """Fused silhouette marking + edge DDA + edge gradient; returns d_pos (B, V, 4), added
+    into ``d_pos`` when given."""
+    _arr(bitset, _i32, 4, name="bitset")
+    _arr(target_bitset, _i32, 4, name="target_bitset")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(edge2tri, _i32, 2, 2, "edge2tri")
+    _arr(edge2cluster, _i32, 1, name="edge2cluster")
+    _cuda(bitset, target_bitset, pos, tri, edges, edge2tri, edge2cluster)
+    B, H, W, S = bitset.shape
+    if tuple(target_bitset.shape) != (B, H, W, S) or pos.shape[0] != B:
+        raise RuntimeError("antialiased_cluster_bitset_grad: bitset, target_bitset and pos views must match.")
+    if edge2tri.shape[0] != edges.shape[0] or edge2cluster.shape[0] < edges.shape[0]:
+        raise RuntimeError("antialiased_cluster_bitset_grad: edge2tri / edge2cluster must cover every edge.")
+    V = pos.shape[1]
+    if d_pos is None:
+        d_pos = torch.zeros_like(pos)
+    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_workspace_size(B, V)
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, pos.device)
+    call("s2c_antialiased_cluster_bitset_grad", B, H, W, S, ptr(bitset), ptr(target_bitset), V, ptr(pos),
+         tri.shape[0], ptr(tri), edges.shape[0], ptr(edges), ptr(edge2tri), ptr(edge2cluster), ptr(d_pos),
+         float(kernel_radius), float(rho), ptr(ws), ws.numel(), _stream(pos))
+    return d_pos
+
+
 # ---- compaction (pystrns2cards.cpp:774-786) ------------------------------------------
 def compact_valid_ints(input, output) -> int:
     _arr(input, _i32, 1, name="input")

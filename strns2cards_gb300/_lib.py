@@ -42,6 +42,8 @@ SIGNATURES = {
     "s2c_compute_fragments": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i64, vp, vp, vp], c_i),
     "s2c_depth_test_workspace_size": ([c_i, c_i, c_i], c_sz),
     "s2c_depth_test": ([c_i, c_i, c_i, c_i64, vp, vp, vp, vp, c_sz, vp], c_i),
+    "s2c_rasterize_fused_workspace_size": ([c_i, c_i, c_i], c_sz),
+    "s2c_rasterize_fused": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_i, c_i, vp, vp, vp, c_sz, vp], c_i),
     "s2c_barycentric_derivatives": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, vp], c_i),
     "s2c_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp], c_i),
     "s2c_backward_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp], c_i),
@@ -55,6 +57,9 @@ SIGNATURES = {
     "s2c_backward_antialiased_cluster_bitset_workspace_size": ([c_i, c_i], c_sz),
     "s2c_backward_antialiased_cluster_bitset_f64": ([c_i64, vp, vp, c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp,
                                                      vp, vp, c_f, c_f, vp, c_sz, vp], c_i),
+    "s2c_antialiased_cluster_bitset_grad_workspace_size": ([c_i, c_i], c_sz),
+    "s2c_antialiased_cluster_bitset_grad": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, c_f,
+                                             c_f, vp, c_sz, vp], c_i),
     "s2c_compact_valid_ints_workspace_size": ([c_i64], c_sz),
     "s2c_compact_valid_ints": ([c_i64, vp, vp, vp, c_sz, i64p, vp], c_i),
     "s2c_popcount_bitset": ([c_i64, c_i, vp, vp, vp], c_i),

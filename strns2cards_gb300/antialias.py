@@ -65,16 +65,26 @@ def antialiased_cluster_bitset_grad(
     edge2cluster: torch.Tensor,
     kernel_radius: float = 7.0,
     rho: float = 1.0,
+    fused: bool = True,
 ) -> torch.Tensor:
-    """``d_pos`` (B, V, 4) of ``antialiased_cluster_bitset_loss`` (``antialias.py:100-122``)."""
-    _, H, W, _ = target_bitset.shape
-    prim_ids, normals = mark_discontinuity_edges((H, W), pos, tri, edges, edge2tri)
-    frag_pix, frag_attrs = dda_compute_fragments((H, W), pos.contiguous(), edges.contiguous(), prim_ids)
-    d_pos = torch.zeros_like(pos)
-    _core.backward_antialiased_cluster_bitset(frag_pix, frag_attrs, bitset.contiguous(), target_bitset.contiguous(),
-                                              pos.contiguous(), edges.contiguous(), normals, edge2cluster.contiguous(),
-                                              d_pos, kernel_radius, rho)
-    return d_pos
+    """``d_pos`` (B, V, 4) of ``antialiased_cluster_bitset_loss`` (``antialias.py:100-122``).
+
+    ``fused`` (default): one pass per (view, edge) without a fragment list or host
+    synchronisation.  ``fused=False``: the reference's sequence of ops
+    (mark_discontinuity_edges, dda_compute_fragments, backward_antialiased_cluster_bitset).
+    """
+    _, H, W, S = target_bitset.shape
+    if not fused:
+        prim_ids, normals = mark_discontinuity_edges((H, W), pos, tri, edges, edge2tri)
+        frag_pix, frag_attrs = dda_compute_fragments((H, W), pos.contiguous(), edges.contiguous(), prim_ids)
+        d_pos = torch.zeros_like(pos)
+        _core.backward_antialiased_cluster_bitset(frag_pix, frag_attrs, bitset.contiguous(),
+                                                  target_bitset.contiguous(), pos.contiguous(), edges.contiguous(),
+                                                  normals, edge2cluster.contiguous(), d_pos, kernel_radius, rho)
+        return d_pos
+    return _core.antialiased_cluster_bitset_grad(bitset.contiguous(), target_bitset.contiguous(), pos.contiguous(),
+                                                 tri.contiguous(), edges.contiguous(), edge2tri.contiguous(),
+                                                 edge2cluster.contiguous(), kernel_radius, rho)
 
 
 def antialiased_cluster_bitset_loss(

@@ -33,22 +33,18 @@ __device__ __forceinline__ float2 ndc_a(float4 p) {
     return make_float2(__fadd_rn(1.f, __fdiv_rn(p.x, p.w)), __fsub_rn(1.f, __fdiv_rn(p.y, p.w)));
 }
 
-// antialias.cu:38-94
-__global__ void __launch_bounds__(256) mark_edges_kernel(int H, int W, int B, Mesh M, int32_t* __restrict__ prim_ids,
-                                                         float2* __restrict__ normals) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)B * M.E) return;
-    const int b = (int)M.divE.div((uint32_t)idx);
-    const int e = (int)idx - b * M.E;
+// antialias.cu:38-94 for edge e of view b: 0 = zero-length edge (no normal), 1 = normal
+// only, 2 = silhouette or boundary edge (marked) with its oriented normal
+__device__ __forceinline__ int mark_edge(int H, int W, const Mesh& M, int b, int e, float2& nrm) {
     const int2 ev = __ldg(M.edges + e);
-    if ((unsigned)ev.x >= (unsigned)M.V || (unsigned)ev.y >= (unsigned)M.V) return;
+    if ((unsigned)ev.x >= (unsigned)M.V || (unsigned)ev.y >= (unsigned)M.V) return 0;
     const float4* pb = M.pos4 + (int64_t)b * M.V;
     const float hh = __fmul_rn((float)H, 0.5f), hw = __fmul_rn((float)W, 0.5f);
     const float2 a0 = ndc_a(__ldg(pb + ev.x)), a1 = ndc_a(__ldg(pb + ev.y));
     const float x0 = __fmul_rn(hw, a0.x), y0 = __fmul_rn(hh, a0.y);
     const float dx = __fmaf_rn(hw, a1.x, -x0), dy = __fmaf_rn(hh, a1.y, -y0);
     const float len = __fsqrt_rn(__fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-    if (len == 0.f) return;
+    if (len == 0.f) return 0;
     const float nx = __fdiv_rn(-dy, len), ny = __fdiv_rn(dx, len);
     float d[2] = {0.f, 0.f};
     const int2 tt = __ldg(M.e2t + e);
@@ -61,9 +57,21 @@ __global__ void __launch_bounds__(256) mark_edges_kernel(int H, int W, int B, Me
         const float2 a2 = ndc_a(__ldg(pb + v2));
         d[i] = __fmaf_rn(nx, __fmaf_rn(hw, a2.x, -x0), __fmul_rn(ny, __fmaf_rn(hh, a2.y, -y0)));
     }
-    if (__fmul_rn(d[0], d[1]) >= 0.f) prim_ids[idx] = (int32_t)idx;
     const float sign = __fmul_rn(2.f, __fsub_rn(0.5f, (float)(d[0] > 0.f || d[1] > 0.f)));
-    normals[idx] = make_float2(__fmul_rn(sign, nx), __fmul_rn(sign, ny));
+    nrm = make_float2(__fmul_rn(sign, nx), __fmul_rn(sign, ny));
+    return __fmul_rn(d[0], d[1]) >= 0.f ? 2 : 1;
+}
+
+__global__ void __launch_bounds__(256) mark_edges_kernel(int H, int W, int B, Mesh M, int32_t* __restrict__ prim_ids,
+                                                         float2* __restrict__ normals) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)B * M.E) return;
+    const int b = (int)M.divE.div((uint32_t)idx);
+    const int e = (int)idx - b * M.E;
+    float2 nrm;
+    const int m = mark_edge(H, W, M, b, e, nrm);
+    if (m == 2) prim_ids[idx] = (int32_t)idx;
+    if (m >= 1) normals[idx] = nrm;
 }
 
 struct AAArgs {
@@ -87,109 +95,198 @@ __device__ __forceinline__ int bit_of(const int32_t* __restrict__ bits, int64_t 
     return (__ldg(bits + pix * S + (c >> 5)) >> (c & 31)) & 1;
 }
 
-// antialias.cu:121-279, one warp per fragment
+// The window part of antialias.cu:121-279 for one fragment (view b, pixel (h, w), sweep
+// axis, t1, edge e), evaluated by a whole warp: every lane computes the (uniform) set-up,
+// the lanes share the taps, and the FP64 window sum is reduced over the warp.  Returns
+// false when the fragment contributes nothing; otherwise dc (on every lane) and the
+// quantities of the chain rule.
+struct AAFrag {
+    double dc;
+    float px, py, pw, t0, t1;
+    float2 nrm;
+    int2 ev;
+};
+
+__device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w, float axis, float t1, int e,
+                                            float2 nrm, int lane, AAFrag& o) {
+    const float fH = (float)A.H, fW = (float)A.W;
+    if (e < 0 || e >= A.E || b < 0 || b >= A.B || h < 0 || h >= A.H || w < 0 || w >= A.W) return false;
+    const float t0 = __fsub_rn(1.f, t1);
+    const int2 ev = __ldg(A.edges + e);
+    if ((unsigned)ev.x >= (unsigned)A.V || (unsigned)ev.y >= (unsigned)A.V) return false;
+    const float4 p0 = __ldg(A.pos4 + (int64_t)b * A.V + ev.x), p1 = __ldg(A.pos4 + (int64_t)b * A.V + ev.y);
+    const float px = __fmaf_rn(t0, p0.x, __fmul_rn(t1, p1.x));
+    const float py = __fmaf_rn(t0, p0.y, __fmul_rn(t1, p1.y));
+    const float pw = __fmaf_rn(t0, p0.w, __fmul_rn(t1, p1.w));
+    const float fx = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(1.f, __fdiv_rn(px, pw))), fW);
+    const float fy = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(1.f, __fdiv_rn(py, pw))), fH);
+    const float rx = __fsub_rn(fx, floorf(fx)), ry = __fsub_rn(fy, floorf(fy));
+    int nh = h, nw = w;
+    float dot;
+    if (axis == 0.f) {
+        if (!isfinite(rx) || fabsf(__fsub_rn(rx, 0.5f)) >= 1e-4f) return false;
+        const int d = 2 * (int)(ry > 0.5f) - 1;
+        nh += d;
+        dot = __fmul_rn((float)d, nrm.y);
+    } else {
+        if (!isfinite(ry) || fabsf(__fsub_rn(ry, 0.5f)) >= 1e-4f) return false;
+        const int d = 2 * (int)(rx > 0.5f) - 1;
+        nw += d;
+        dot = __fmul_rn((float)d, nrm.x);
+    }
+    if (nw < 0 || nw >= A.W || nh < 0 || nh >= A.H || dot == 0.f) return false;
+    const int c = __ldg(A.e2c + e);
+    if (c < 0 || c >= 32 * A.S) return false;
+    const int64_t img = (int64_t)b * A.H * A.W;
+    const int c01 = 1 - (dot > 0.f ? bit_of(A.bitset, img + (int64_t)nh * A.W + nw, A.S, c)
+                                   : bit_of(A.bitset, img + (int64_t)h * A.W + w, A.S, c));
+    if (c01 == 0) return false;
+    // Gaussian window (antialias.cu:121-176), taps spread over the warp
+    const int R = f2i(floorf(A.kr));
+    const int cw = f2i(floorf(fx)), ch = f2i(floorf(fy));
+    const int h0 = max(ch - R, 0), h1 = min(ch + R, A.H - 1) + 1;
+    const int w0 = max(cw - R, 0), w1 = min(cw + R, A.W - 1) + 1;
+    const int ww = w1 - w0, taps = ww > 0 && h1 > h0 ? ww * (h1 - h0) : 0;
+    const float sigma = __fdiv_rn(A.kr, 4.f);
+    const float cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
+    const float alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
+    const float kr2 = __fmul_rn(A.kr, A.kr);
+    double acc = 0.0;
+    for (int j = lane; j < taps; j += 32) {
+        const int th = h0 + j / ww, tw = w0 + j % ww;
+        const int64_t pix = img + (int64_t)th * A.W + tw;
+        const int c0 = bit_of(A.bitset, pix, A.S, c), c1 = bit_of(A.target, pix, A.S, c);
+        if (c0 == c1) continue;
+        const float dx = __fsub_rn(__fadd_rn((float)tw, 0.5f), fx);
+        const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), fy);
+        const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+        if (!(n2 < kr2)) continue;
+        const double wgt = (double)cc * (double)expf(-alpha * n2);
+        acc += wgt * (double)(c0 - c1) * (c1 == 0 ? (double)A.rho : 1.0);
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    o.dc = (double)c01 * acc;
+    if (o.dc == 0.0) return false;
+    o.px = px;
+    o.py = py;
+    o.pw = pw;
+    o.t0 = t0;
+    o.t1 = t1;
+    o.nrm = nrm;
+    o.ev = ev;
+    return true;
+}
+
+// FP64 chain rule of one fragment: (d/dx, d/dy, d/dw) of the edge point, false if not finite
+__device__ __forceinline__ bool aa_chain64(const AAArgs& A, const AAFrag& f, double& qx, double& qy, double& qw) {
+    const double dxd = f.dc * 0.5 * (double)A.W * (double)f.nrm.x;
+    const double dyd = f.dc * -0.5 * (double)A.H * (double)f.nrm.y;
+    const double pwd = (double)f.pw;
+    qx = dxd / pwd;
+    qy = dyd / pwd;
+    qw = (dxd * (double)f.px + dyd * (double)f.py) / (pwd * pwd);
+    return isfinite(qx) && isfinite(qy) && isfinite(qw);
+}
+
+// antialias.cu:121-279, one warp per fragment of a fragment list
 __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const float fH = (float)A.H, fW = (float)A.W;
     for (int64_t i = warp0; i < A.F; i += nwarps) {
-        // every lane evaluates the (uniform) fragment set-up
-        const int b = A.frag_pix[3 * i], h = A.frag_pix[3 * i + 1], w = A.frag_pix[3 * i + 2];
         const float4 fa = A.frag_attrs[i];
-        const int e = f2i(fa.w) - 1;
-        if (e < 0 || e >= A.E || b < 0 || b >= A.B || h < 0 || h >= A.H || w < 0 || w >= A.W) continue;
-        const float t1 = fa.y, t0 = __fsub_rn(1.f, t1);
-        const int2 ev = __ldg(A.edges + e);
-        if ((unsigned)ev.x >= (unsigned)A.V || (unsigned)ev.y >= (unsigned)A.V) continue;
-        const float4 p0 = __ldg(A.pos4 + (int64_t)b * A.V + ev.x), p1 = __ldg(A.pos4 + (int64_t)b * A.V + ev.y);
-        const float px = __fmaf_rn(t0, p0.x, __fmul_rn(t1, p1.x));
-        const float py = __fmaf_rn(t0, p0.y, __fmul_rn(t1, p1.y));
-        const float pw = __fmaf_rn(t0, p0.w, __fmul_rn(t1, p1.w));
-        const float fx = __fmul_rn(__fmul_rn(0.5f, __fadd_rn(1.f, __fdiv_rn(px, pw))), fW);
-        const float fy = __fmul_rn(__fmul_rn(0.5f, __fsub_rn(1.f, __fdiv_rn(py, pw))), fH);
-        const float2 nrm = __ldg(A.normals + (int64_t)b * A.E + e);
-        const float rx = __fsub_rn(fx, floorf(fx)), ry = __fsub_rn(fy, floorf(fy));
-        int nh = h, nw = w;
-        float dot;
-        if (fa.x == 0.f) {
-            if (!isfinite(rx) || fabsf(__fsub_rn(rx, 0.5f)) >= 1e-4f) continue;
-            const int d = 2 * (int)(ry > 0.5f) - 1;
-            nh += d;
-            dot = __fmul_rn((float)d, nrm.y);
-        } else {
-            if (!isfinite(ry) || fabsf(__fsub_rn(ry, 0.5f)) >= 1e-4f) continue;
-            const int d = 2 * (int)(rx > 0.5f) - 1;
-            nw += d;
-            dot = __fmul_rn((float)d, nrm.x);
-        }
-        if (nw < 0 || nw >= A.W || nh < 0 || nh >= A.H || dot == 0.f) continue;
-        const int c = __ldg(A.e2c + e);
-        if (c < 0 || c >= 32 * A.S) continue;
-        const int64_t img = (int64_t)b * A.H * A.W;
-        const int c01 = 1 - (dot > 0.f ? bit_of(A.bitset, img + (int64_t)nh * A.W + nw, A.S, c)
-                                       : bit_of(A.bitset, img + (int64_t)h * A.W + w, A.S, c));
-        if (c01 == 0) continue;
-        // Gaussian window (antialias.cu:121-176), taps spread over the warp
-        const int R = f2i(floorf(A.kr));
-        const int cw = f2i(floorf(fx)), ch = f2i(floorf(fy));
-        const int h0 = max(ch - R, 0), h1 = min(ch + R, A.H - 1) + 1;
-        const int w0 = max(cw - R, 0), w1 = min(cw + R, A.W - 1) + 1;
-        const int ww = w1 - w0, taps = ww > 0 && h1 > h0 ? ww * (h1 - h0) : 0;
-        const float sigma = __fdiv_rn(A.kr, 4.f);
-        const float cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
-        const float alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
-        const float kr2 = __fmul_rn(A.kr, A.kr);
-        double acc = 0.0;
-        for (int j = lane; j < taps; j += 32) {
-            const int th = h0 + j / ww, tw = w0 + j % ww;
-            const int64_t pix = img + (int64_t)th * A.W + tw;
-            const int c0 = bit_of(A.bitset, pix, A.S, c), c1 = bit_of(A.target, pix, A.S, c);
-            if (c0 == c1) continue;
-            const float dx = __fsub_rn(__fadd_rn((float)tw, 0.5f), fx);
-            const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), fy);
-            const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-            if (!(n2 < kr2)) continue;
-            const double wgt = (double)cc * (double)expf(-alpha * n2);
-            acc += wgt * (double)(c0 - c1) * (c1 == 0 ? (double)A.rho : 1.0);
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        const int fb = A.frag_pix[3 * i], fe = f2i(fa.w) - 1;
+        if (fe < 0 || fe >= A.E || fb < 0 || fb >= A.B) continue;
+        AAFrag f;
+        if (!aa_fragment(A, fb, A.frag_pix[3 * i + 1], A.frag_pix[3 * i + 2], fa.x, fa.y, fe,
+                         __ldg(A.normals + (int64_t)fb * A.E + fe), lane, f))
+            continue;
         if (lane != 0) continue;
-        const double dc = (double)c01 * acc;
-        if (dc == 0.0) continue;
         if (A.acc64) {
             // chain rule and accumulation in FP64 (no cancellation loss across fragments)
-            const double dxd = dc * 0.5 * (double)fW * (double)nrm.x;
-            const double dyd = dc * -0.5 * (double)fH * (double)nrm.y;
-            const double pwd = (double)pw;
-            const double qx = dxd / pwd, qy = dyd / pwd;
-            const double qw = (dxd * (double)px + dyd * (double)py) / (pwd * pwd);
-            if (!isfinite(qx) || !isfinite(qy) || !isfinite(qw)) continue;
-            double* a0 = A.acc64 + ((int64_t)b * A.V + ev.x) * 3;
-            double* a1 = A.acc64 + ((int64_t)b * A.V + ev.y) * 3;
-            atomicAdd(a0 + 0, qx * (double)t0);
-            atomicAdd(a0 + 1, qy * (double)t0);
-            atomicAdd(a0 + 2, qw * (double)t0);
-            atomicAdd(a1 + 0, qx * (double)t1);
-            atomicAdd(a1 + 1, qy * (double)t1);
-            atomicAdd(a1 + 2, qw * (double)t1);
+            double qx, qy, qw;
+            if (!aa_chain64(A, f, qx, qy, qw)) continue;
+            const int b = A.frag_pix[3 * i];
+            double* a0 = A.acc64 + ((int64_t)b * A.V + f.ev.x) * 3;
+            double* a1 = A.acc64 + ((int64_t)b * A.V + f.ev.y) * 3;
+            atomicAdd(a0 + 0, qx * (double)f.t0);
+            atomicAdd(a0 + 1, qy * (double)f.t0);
+            atomicAdd(a0 + 2, qw * (double)f.t0);
+            atomicAdd(a1 + 0, qx * (double)f.t1);
+            atomicAdd(a1 + 1, qy * (double)f.t1);
+            atomicAdd(a1 + 2, qw * (double)f.t1);
             continue;
         }
-        const float dcf = (float)dc;
-        const float dx = __fmul_rn(__fmul_rn(__fmul_rn(dcf, 0.5f), fW), nrm.x);
-        const float dy = __fmul_rn(__fmul_rn(__fmul_rn(dcf, -0.5f), fH), nrm.y);
-        const float dpx = __fdiv_rn(dx, pw), dpy = __fdiv_rn(dy, pw);
-        const float dpw = __fdiv_rn(__fmaf_rn(dx, px, __fmul_rn(dy, py)), __fmul_rn(pw, pw));
+        // FP32 chain rule and float atomics, as the reference
+        const float dcf = (float)f.dc;
+        const float dx = __fmul_rn(__fmul_rn(__fmul_rn(dcf, 0.5f), (float)A.W), f.nrm.x);
+        const float dy = __fmul_rn(__fmul_rn(__fmul_rn(dcf, -0.5f), (float)A.H), f.nrm.y);
+        const float dpx = __fdiv_rn(dx, f.pw), dpy = __fdiv_rn(dy, f.pw);
+        const float dpw = __fdiv_rn(__fmaf_rn(dx, f.px, __fmul_rn(dy, f.py)), __fmul_rn(f.pw, f.pw));
         if (!isfinite(dpx) || !isfinite(dpy) || !isfinite(dpw)) continue;
-        float* g0 = A.d_pos + ((int64_t)b * A.V + ev.x) * 4;
-        float* g1 = A.d_pos + ((int64_t)b * A.V + ev.y) * 4;
-        atomicAdd(g0 + 0, __fmul_rn(dpx, t0));
-        atomicAdd(g0 + 1, __fmul_rn(dpy, t0));
-        atomicAdd(g0 + 3, __fmul_rn(dpw, t0));
-        atomicAdd(g1 + 0, __fmul_rn(dpx, t1));
-        atomicAdd(g1 + 1, __fmul_rn(dpy, t1));
-        atomicAdd(g1 + 3, __fmul_rn(dpw, t1));
+        const int b = A.frag_pix[3 * i];
+        float* g0 = A.d_pos + ((int64_t)b * A.V + f.ev.x) * 4;
+        float* g1 = A.d_pos + ((int64_t)b * A.V + f.ev.y) * 4;
+        atomicAdd(g0 + 0, __fmul_rn(dpx, f.t0));
+        atomicAdd(g0 + 1, __fmul_rn(dpy, f.t0));
+        atomicAdd(g0 + 3, __fmul_rn(dpw, f.t0));
+        atomicAdd(g1 + 0, __fmul_rn(dpx, f.t1));
+        atomicAdd(g1 + 1, __fmul_rn(dpy, f.t1));
+        atomicAdd(g1 + 3, __fmul_rn(dpw, f.t1));
+    }
+}
+
+// Fused edge gradient: one warp per (view, edge).  The mark test, the edge's DDA walk
+// (the fragments dda_compute_fragments + filter_valid_fragments would list) and each
+// fragment's window run in registers; the edge's contributions are summed in FP64 and
+// added to the FP64 accumulator once per edge.  No fragment list, no host round trip.
+__global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int64_t BE = (int64_t)A.B * M.E;
+    for (int64_t pe = warp0; pe < BE; pe += nwarps) {
+        const int b = (int)M.divE.div((uint32_t)pe);
+        const int e = (int)pe - b * M.E;
+        float2 nrm;
+        if (mark_edge(A.H, A.W, M, b, e, nrm) != 2) continue;
+        const int2 ev = __ldg(M.edges + e);
+        const float4 p0 = __ldg(M.pos4 + (int64_t)b * M.V + ev.x), p1 = __ldg(M.pos4 + (int64_t)b * M.V + ev.y);
+        const Span sp = dda_span(p0, p1, A.H, A.W);
+        const int ee = prim_roundtrip(e);
+        double s0x = 0.0, s0y = 0.0, s0w = 0.0, s1x = 0.0, s1y = 0.0, s1w = 0.0;
+        bool any = false;
+        for (int k = 0; k < sp.count; ++k) {
+            float x, y;
+            dda_sample(sp, k, x, y);
+            const int h = f2i(floorf(y)), w = f2i(floorf(x));
+            if (h < 0 || h >= A.H || w < 0 || w >= A.W) continue;
+            const float t1 = dda_t1(p0, p1, x, y, sp.axis, A.H, A.W);
+            if (!z_ok(dda_z(p0, p1, t1))) continue;
+            AAFrag f;
+            if (!aa_fragment(A, b, h, w, sp.axis, t1, ee, nrm, lane, f)) continue;
+            double qx, qy, qw;
+            if (!aa_chain64(A, f, qx, qy, qw)) continue;
+            s0x += qx * (double)f.t0;
+            s0y += qy * (double)f.t0;
+            s0w += qw * (double)f.t0;
+            s1x += qx * (double)f.t1;
+            s1y += qy * (double)f.t1;
+            s1w += qw * (double)f.t1;
+            any = true;
+        }
+        if (lane == 0 && any) {
+            const int2 evv = __ldg(A.edges + ee);
+            double* a0 = A.acc64 + ((int64_t)b * A.V + evv.x) * 3;
+            double* a1 = A.acc64 + ((int64_t)b * A.V + evv.y) * 3;
+            atomicAdd(a0 + 0, s0x);
+            atomicAdd(a0 + 1, s0y);
+            atomicAdd(a0 + 2, s0w);
+            atomicAdd(a1 + 0, s1x);
+            atomicAdd(a1 + 1, s1y);
+            atomicAdd(a1 + 2, s1w);
+        }
     }
 }
 
@@ -309,4 +406,67 @@ extern "C" s2c_status s2c_backward_antialiased_cluster_bitset_f64(
     S2C_REQUIRE(workspace, "backward_antialiased_cluster_bitset_f64: null workspace");
     return aa_backward(F, frag_pix, frag_attrs, B, H, W, S, bitset, target, V, pos, E, edges, normals, edge2cluster,
                        d_pos, kernel_radius, rho, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V) {
+    return (size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3 * sizeof(double);
+}
+
+extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, int S, const int32_t* bitset,
+                                                          const int32_t* target, int V, const float* pos, int T,
+                                                          const int32_t* tri, int E, const int32_t* edges,
+                                                          const int32_t* edge2tri, const int32_t* edge2cluster,
+                                                          float* d_pos, float kernel_radius, float rho,
+                                                          void* workspace, size_t workspace_bytes,
+                                                          s2c_stream stream) {
+    S2C_REQUIRE(B > 0 && H > 0 && W > 0 && S > 0 && V >= 0 && T >= 0 && E >= 0,
+                "antialiased_cluster_bitset_grad: bad sizes");
+    const int64_t BE = (int64_t)B * E, BV = (int64_t)B * V;
+    S2C_REQUIRE(BE < (1LL << 31), "antialiased_cluster_bitset_grad: B*E too large");
+    if (BE == 0 || BV == 0) return S2C_OK;
+    S2C_REQUIRE(bitset && target && pos && edges && edge2tri && edge2cluster && d_pos && (T == 0 || tri) && workspace,
+                "antialiased_cluster_bitset_grad: null pointer");
+    S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && ((uintptr_t)edges & 7) == 0 && ((uintptr_t)edge2tri & 7) == 0 &&
+                    ((uintptr_t)workspace & 7) == 0,
+                "antialiased_cluster_bitset_grad: misaligned");
+    S2C_REQUIRE(kernel_radius >= 0.f && kernel_radius < 1024.f, "antialiased_cluster_bitset_grad: bad kernel_radius");
+    S2C_REQUIRE(workspace_bytes >= (size_t)BV * 3 * sizeof(double),
+                "antialiased_cluster_bitset_grad: workspace of %zu bytes, need %lld", workspace_bytes,
+                (long long)(BV * 3 * sizeof(double)));
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(workspace, 0, (size_t)BV * 3 * sizeof(double), st);
+    if (e != cudaSuccess) return cuda_status(e, "antialiased_cluster_bitset_grad: memset");
+    Mesh M;
+    M.pos4 = (const float4*)pos;
+    M.tri = tri;
+    M.edges = (const int2*)edges;
+    M.e2t = (const int2*)edge2tri;
+    M.V = V;
+    M.T = T;
+    M.E = E;
+    M.divE = FastDiv((uint32_t)E);
+    AAArgs A{};
+    A.F = 0;
+    A.B = B;
+    A.H = H;
+    A.W = W;
+    A.S = S;
+    A.bitset = bitset;
+    A.target = target;
+    A.pos4 = (const float4*)pos;
+    A.V = V;
+    A.E = E;
+    A.edges = (const int2*)edges;
+    A.normals = nullptr;
+    A.e2c = edge2cluster;
+    A.d_pos = d_pos;
+    A.acc64 = (double*)workspace;
+    A.kr = kernel_radius;
+    A.rho = rho;
+    const int64_t warps = std::min<int64_t>(BE, (int64_t)num_sms() * 64);
+    aa_fused_kernel<<<grid_for(warps * 32, 256), 256, 0, st>>>(A, M);
+    S2C_CHECK_LAUNCH("aa_fused_kernel");
+    aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, (const double*)workspace, d_pos);
+    S2C_CHECK_LAUNCH("aa_finalize_kernel");
+    return S2C_OK;
 }

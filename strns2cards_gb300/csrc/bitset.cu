@@ -78,36 +78,79 @@ __global__ void __launch_bounds__(256) xor_popcount_kernel(int64_t nwords, const
 }
 
 // per-cluster pixel counts of a & b and a | b (per-card IoU = inter / union)
+// Per-cluster pixel counts of a & b and a | b.  Each thread keeps one slot s for its whole
+// run (its word stride is a multiple of S), so the 32 clusters of that slot are counted
+// positionally in registers: 4-bit counters per bit (x >> r) & 0x11111111 for r = 0..3,
+// spread into 8-bit counters every 15 words, and those added to the block's per-cluster
+// counters every 255 words; the block's counters go to the global uint64 totals once.
+__device__ __forceinline__ void iou_nib_flush(uint32_t* n, uint32_t* b) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        b[2 * r] += n[r] & 0x0F0F0F0Fu;
+        b[2 * r + 1] += (n[r] >> 4) & 0x0F0F0F0Fu;
+        n[r] = 0u;
+    }
+}
+
+// byte k of b[2r + h] counts bit 8k + 4h + r
+__device__ __forceinline__ void iou_byte_flush(uint32_t* b, unsigned int* hist, unsigned long long* glob, int base,
+                                               int K) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int r = q >> 1, h = q & 1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint32_t cnt = (b[q] >> (8 * k)) & 0xFFu;
+            const int c = base + 8 * k + 4 * h + r;
+            if (cnt && c < K) {
+                if (hist) atomicAdd(hist + c, cnt);
+                else atomicAdd(glob + c, (unsigned long long)cnt);
+            }
+        }
+        b[q] = 0u;
+    }
+}
+
 __global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, int K, const int32_t* __restrict__ a,
                                                           const int32_t* __restrict__ b,
                                                           unsigned long long* __restrict__ inter,
-                                                          unsigned long long* __restrict__ uni, int use_smem) {
-    extern __shared__ unsigned int hist[];  // 2K counters when use_smem
+                                                          unsigned long long* __restrict__ uni, int use_smem,
+                                                          int64_t tstride) {
+    extern __shared__ unsigned int hist[];  // inter[K] | union[K] when use_smem
     if (use_smem) {
         for (int i = threadIdx.x; i < 2 * K; i += blockDim.x) hist[i] = 0u;
         __syncthreads();
     }
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nwords = npix * S;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nwords; i += stride) {
-        const uint32_t x = (uint32_t)__ldcs(a + i), y = (uint32_t)__ldcs(b + i);
-        uint32_t u = x | y;
-        if (!u) continue;
-        const uint32_t both = x & y;
-        const int base = (int)(i % S) * 32;
-        while (u) {
-            const int j = __ffs(u) - 1;
-            u &= u - 1;
-            const int c = base + j;
-            if (c >= K) continue;
-            if (use_smem) {
-                atomicAdd(hist + K + c, 1u);
-                if ((both >> j) & 1) atomicAdd(hist + c, 1u);
-            } else {
-                atomicAdd(uni + c, 1ull);
-                if ((both >> j) & 1) atomicAdd(inter + c, 1ull);
+    if (t < tstride) {
+        const int base = (int)(t % S) * 32;
+        uint32_t nI[4] = {0u, 0u, 0u, 0u}, nU[4] = {0u, 0u, 0u, 0u};
+        uint32_t bI[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u}, bU[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        int cn = 0, cb = 0;
+        for (int64_t i = t; i < nwords; i += tstride) {
+            const uint32_t x = (uint32_t)__ldcs(a + i), y = (uint32_t)__ldcs(b + i);
+            const uint32_t ia = x & y, ua = x | y;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                nI[r] += (ia >> r) & 0x11111111u;
+                nU[r] += (ua >> r) & 0x11111111u;
+            }
+            if (++cn == 15) {
+                cn = 0;
+                iou_nib_flush(nI, bI);
+                iou_nib_flush(nU, bU);
+                if (++cb == 17) {
+                    cb = 0;
+                    iou_byte_flush(bI, use_smem ? hist : nullptr, inter, base, K);
+                    iou_byte_flush(bU, use_smem ? hist + K : nullptr, uni, base, K);
+                }
             }
         }
+        iou_nib_flush(nI, bI);
+        iou_nib_flush(nU, bU);
+        iou_byte_flush(bI, use_smem ? hist : nullptr, inter, base, K);
+        iou_byte_flush(bU, use_smem ? hist + K : nullptr, uni, base, K);
     }
     if (use_smem) {
         __syncthreads();
@@ -148,9 +191,12 @@ extern "C" s2c_status s2c_cluster_iou_counts(int64_t npix, int S, int K, const i
     S2C_REQUIRE(a && b, "cluster_iou_counts: null input");
     const size_t smem = (size_t)2 * K * sizeof(unsigned int);
     const int use_smem = smem <= 48 * 1024;
-    const unsigned grid = (unsigned)std::min<int64_t>((npix * S + 255) / 256, (int64_t)num_sms() * 8);
-    cluster_iou_kernel<<<grid, 256, use_smem ? smem : 0, st>>>(npix, S, K, a, b, (unsigned long long*)inter,
-                                                               (unsigned long long*)uni, use_smem);
+    int64_t grid = std::min<int64_t>((npix * S + 255) / 256, (int64_t)num_sms() * 8);
+    grid = std::max<int64_t>(grid, (S + 255) / 256);
+    // every thread's stride is a whole number of pixels, so its slot never changes
+    const int64_t tstride = (grid * 256 / S) * S;
+    cluster_iou_kernel<<<(unsigned)grid, 256, use_smem ? smem : 0, st>>>(
+        npix, S, K, a, b, (unsigned long long*)inter, (unsigned long long*)uni, use_smem, tstride);
     S2C_CHECK_LAUNCH("cluster_iou_kernel");
     return S2C_OK;
 }

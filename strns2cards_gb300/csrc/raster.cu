@@ -7,6 +7,8 @@
 // position after a compaction whose order depends on block scheduling.  Here the
 // compaction keeps input order, so exact depth ties resolve to the first fragment in
 // (view, triangle, row-major pixel) order, deterministically.
+#include <algorithm>
+
 #include "common.cuh"
 #include "scan.cuh"
 
@@ -19,13 +21,8 @@ struct Tris {
     FastDiv divT;
 };
 
-// rasterize.cu:9-59: screen rectangle of triangle (b, t)
-__global__ void __launch_bounds__(256) tri_rects_kernel(int H, int W, int B, Tris R, int4* __restrict__ rects,
-                                                        int32_t* __restrict__ counts) {
-    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= (int64_t)B * R.T) return;
-    const int b = (int)R.divT.div((uint32_t)idx);
-    const int t = (int)idx - b * R.T;
+// rasterize.cu:9-59: screen rectangle (h0, h_len, w0, w_len) of triangle (b, t)
+__device__ __forceinline__ int4 tri_rect(int H, int W, const Tris& R, int b, int t) {
     const float fH = (float)H, fW = (float)W;
     float x0 = fW, y0 = fH, x1 = 0.f, y1 = 0.f;
     bool bad = false;
@@ -50,8 +47,18 @@ __global__ void __launch_bounds__(256) tri_rects_kernel(int H, int W, int B, Tri
     hl = hl > 0 ? hl : 0;
     wl = wl > 0 ? wl : 0;
     if (bad) hl = wl = 0;  // vertex index out of range: the reference would read out of bounds
-    rects[idx] = make_int4(h0, hl, w0, wl);
-    counts[idx] = (int32_t)((uint32_t)hl * (uint32_t)wl);
+    return make_int4(h0, hl, w0, wl);
+}
+
+__global__ void __launch_bounds__(256) tri_rects_kernel(int H, int W, int B, Tris R, int4* __restrict__ rects,
+                                                        int32_t* __restrict__ counts) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)B * R.T) return;
+    const int b = (int)R.divT.div((uint32_t)idx);
+    const int t = (int)idx - b * R.T;
+    const int4 rc = tri_rect(H, W, R, b, t);
+    rects[idx] = rc;
+    counts[idx] = (int32_t)((uint32_t)rc.y * (uint32_t)rc.w);
 }
 
 // Coverage of pixel (x, y) by a triangle with clip-space corners P0..P2
@@ -149,6 +156,102 @@ __global__ void __launch_bounds__(256) depth_gather_kernel(int64_t npix, const u
     const int fi = (int)(uint32_t)(k & 0xffffffffull);
     if (fi < 0 || fi >= F) return;
     rast[p] = frag_attrs[fi];
+}
+
+// Fused raster (compute_fragments + depth_test + cluster_mask_from_fragments without the
+// fragment list): each warp takes 32 triangles and spreads the pixels of their screen
+// rectangles over its lanes (owner found by a shuffle binary search over the warp's
+// inclusive prefix of rectangle areas).  A covered pixel ORs its cluster bit into the
+// bitset and offers the key (bits(z + 2) << 32 | t) to the pixel's 64-bit minimum:
+// within one pixel the list path's fragment order is triangle order, so the minimum
+// picks the fragment the list-based depth test picks.
+struct FusedRaster {
+    int B, H, W, S;
+    Tris R;
+    const int32_t* __restrict__ t2c;      // nullable
+    int num_t2c;
+    int32_t* __restrict__ bitset;         // nullable
+    unsigned long long* __restrict__ keys;  // nullable
+};
+
+__global__ void __launch_bounds__(256) tri_fused_kernel(FusedRaster F) {
+    const int lane = threadIdx.x & 31;
+    const int64_t BT = (int64_t)F.B * F.R.T;
+    const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t g = warp0 * 32; g < BT; g += nwarps * 32) {
+        const int64_t mine = g + lane;
+        int4 rc = make_int4(0, 0, 0, 0);
+        int b = 0, t = 0;
+        if (mine < BT) {
+            b = (int)F.R.divT.div((uint32_t)mine);
+            t = (int)mine - b * F.R.T;
+            rc = tri_rect(F.H, F.W, F.R, b, t);
+        }
+        // inclusive prefix of the areas over the warp (areas < 2^31 since H, W <= 32768)
+        int64_t pre = (int64_t)rc.y * rc.w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t v = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= o) pre += v;
+        }
+        const int64_t total = __shfl_sync(0xffffffffu, pre, 31);
+        for (int64_t base = 0; base < total; base += 32) {
+            const int64_t j = base + lane;
+            // owner: first lane whose inclusive prefix exceeds j
+            int lo = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int64_t pv = __shfl_sync(0xffffffffu, pre, lo + step - 1);
+                if (pv <= j) lo += step;
+            }
+            const int64_t pv_prev = __shfl_sync(0xffffffffu, pre, lo > 0 ? lo - 1 : 0);
+            const int ob = __shfl_sync(0xffffffffu, b, lo), ot = __shfl_sync(0xffffffffu, t, lo);
+            const int rh0 = __shfl_sync(0xffffffffu, rc.x, lo), rw0 = __shfl_sync(0xffffffffu, rc.z, lo);
+            const int rwl = __shfl_sync(0xffffffffu, rc.w, lo);
+            if (j >= total) continue;
+            const int local = (int)(j - (lo > 0 ? pv_prev : 0));
+            const int y = rh0 + local / rwl, x = rw0 + local % rwl;
+            if (x < 0 || x >= F.W || y < 0 || y >= F.H) continue;
+            const int i0 = __ldg(F.R.tri + 3 * ot), i1 = __ldg(F.R.tri + 3 * ot + 1), i2 = __ldg(F.R.tri + 3 * ot + 2);
+            const float4* pb = F.R.pos4 + (int64_t)ob * F.R.V;
+            float b0, b1, z;
+            if (!tri_cover(F.H, F.W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z)) continue;
+            const int64_t pix = ((int64_t)ob * F.H + y) * F.W + x;
+            if (F.keys) {
+                const float zz = __fadd_rn(z, 2.f);
+                atomicMin(F.keys + pix, ((unsigned long long)(uint32_t)__float_as_int(zz) << 32) | (uint32_t)ot);
+            }
+            if (F.bitset && ot < F.num_t2c) {
+                const int c = __ldg(F.t2c + ot);
+                if (c >= 0 && c < 32 * F.S) atomicOr(F.bitset + pix * F.S + (c >> 5), (int32_t)(1u << (c & 31)));
+            }
+        }
+    }
+}
+
+// rast of the winning triangle of every pixel, recomputed with the forward's arithmetic
+__global__ void __launch_bounds__(256) tri_resolve_kernel(int B, int H, int W, Tris R,
+                                                          const unsigned long long* __restrict__ keys,
+                                                          float4* __restrict__ rast) {
+    const int64_t n = (int64_t)B * H * W;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[p];
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (k != 0xffffffffffffffffull) {
+            const int t = (int)(uint32_t)(k & 0xffffffffull);
+            const int64_t bh = p / W;
+            const int x = (int)(p - bh * W);
+            const int b = (int)(bh / H);
+            const int y = (int)(bh - (int64_t)b * H);
+            const int i0 = __ldg(R.tri + 3 * t), i1 = __ldg(R.tri + 3 * t + 1), i2 = __ldg(R.tri + 3 * t + 2);
+            const float4* pb = R.pos4 + (int64_t)b * R.V;
+            float b0, b1, z;
+            if (tri_cover(H, W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z))
+                o = make_float4(b0, b1, z, (float)(t + 1));
+        }
+        rast[p] = o;
+    }
 }
 
 // rasterize.cu:367-400
@@ -439,5 +542,62 @@ extern "C" s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int 
     dda_interp_backward_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(
         npix, (const float4*)rast, C, d_image, (const int2*)edges, E, V, d_attr);
     S2C_CHECK_LAUNCH("dda_interp_backward_kernel");
+    return S2C_OK;
+}
+
+extern "C" size_t s2c_rasterize_fused_workspace_size(int B, int H, int W) {
+    return (size_t)(B > 0 ? B : 0) * (size_t)(H > 0 ? H : 0) * (size_t)(W > 0 ? W : 0) * 8 + 256;
+}
+
+extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
+                                          const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
+                                          float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream) {
+    S2C_REQUIRE(B > 0 && H > 0 && W > 0 && H <= 32768 && W <= 32768 && V >= 0 && T >= 0,
+                "rasterize_fused: bad sizes");
+    S2C_REQUIRE((int64_t)B * T < (1LL << 31), "rasterize_fused: B*T too large");
+    S2C_REQUIRE(!bitset || (S > 0 && (tri2cluster || num_tri2cluster == 0)), "rasterize_fused: bitset needs S and tri2cluster");
+    S2C_REQUIRE(pos && (T == 0 || tri), "rasterize_fused: null input");
+    S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && (!rast || ((uintptr_t)rast & 15) == 0), "rasterize_fused: misaligned");
+    const int64_t npix = (int64_t)B * H * W;
+    cudaStream_t st = (cudaStream_t)stream;
+    unsigned long long* keys = nullptr;
+    if (rast) {
+        S2C_REQUIRE(workspace && workspace_bytes >= (size_t)npix * 8 && ((uintptr_t)workspace & 7) == 0,
+                    "rasterize_fused: workspace of %zu bytes, need %lld", workspace_bytes, (long long)(npix * 8));
+        keys = (unsigned long long*)workspace;
+        cudaError_t e = cudaMemsetAsync(keys, 0xff, (size_t)npix * 8, st);
+        if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset keys");
+    }
+    if (bitset) {
+        cudaError_t e = cudaMemsetAsync(bitset, 0, (size_t)npix * S * 4, st);
+        if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset bitset");
+    }
+    Tris R;
+    R.pos4 = (const float4*)pos;
+    R.tri = tri;
+    R.V = V;
+    R.T = T;
+    R.divT = FastDiv((uint32_t)(T > 0 ? T : 1));
+    const int64_t BT = (int64_t)B * T;
+    if (BT > 0 && (rast || bitset)) {
+        FusedRaster F;
+        F.B = B;
+        F.H = H;
+        F.W = W;
+        F.S = S;
+        F.R = R;
+        F.t2c = tri2cluster;
+        F.num_t2c = num_tri2cluster;
+        F.bitset = bitset;
+        F.keys = keys;
+        const int64_t warps = std::min<int64_t>((BT + 31) / 32, (int64_t)num_sms() * 64);
+        tri_fused_kernel<<<grid_for(warps * 32, 256), 256, 0, st>>>(F);
+        S2C_CHECK_LAUNCH("tri_fused_kernel");
+    }
+    if (rast) {
+        tri_resolve_kernel<<<grid_for(npix, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(B, H, W, R, keys,
+                                                                                           (float4*)rast);
+        S2C_CHECK_LAUNCH("tri_resolve_kernel");
+    }
     return S2C_OK;
 }

@@ -62,10 +62,48 @@ def depth_test(B: int, resolution: Tuple[int, int], frag_pix: torch.Tensor, frag
     return rast
 
 
+def rasterize_fused(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.Tensor,
+                    tri2cluster: Optional[torch.Tensor] = None, num_clusters: int = 0, want_rast: bool = True,
+                    rast: Optional[torch.Tensor] = None, bitset: Optional[torch.Tensor] = None,
+                    workspace: Optional[torch.Tensor] = None):
+    """One pass of compute_fragments + depth_test (+ cluster_mask_from_fragments when
+    ``tri2cluster`` is given) with no fragment list and no host synchronisation.
+    Returns (rast or None, bitset or None); outputs may be passed in to reuse memory."""
+    if not (pos.is_cuda and tri.is_cuda):
+        raise ValueError("Input tensors must be on CUDA.")
+    if pos.dtype != torch.float32 or pos.ndim != 3 or pos.shape[-1] != 4:
+        raise ValueError("pos must be float32 (B, V, 4).")
+    if tri.dtype != torch.int32 or tri.ndim != 2 or tri.shape[1] != 3:
+        raise ValueError("tri must be int32 (T, 3).")
+    H, W = resolution
+    B, V = pos.shape[0], pos.shape[1]
+    dev = pos.device
+    p, t = pos.contiguous(), tri.contiguous()
+    S = 0
+    if tri2cluster is not None:
+        S = (int(num_clusters) + 31) // 32
+        if S <= 0:
+            raise ValueError("num_clusters must be positive with tri2cluster.")
+        tri2cluster = tri2cluster.contiguous()
+        if bitset is None:
+            bitset = torch.empty((B, H, W, S), dtype=torch.int32, device=dev)
+    if want_rast and rast is None:
+        rast = torch.empty((B, H, W, 4), dtype=torch.float32, device=dev)
+    if not want_rast:
+        rast = None
+    need = _lib.lib().s2c_rasterize_fused_workspace_size(B, H, W) if want_rast else 0
+    if want_rast and (workspace is None or workspace.numel() < need):
+        workspace = _lib.workspace(need, dev)
+    _lib.call("s2c_rasterize_fused", B, H, W, V, _lib.ptr(p), t.shape[0], _lib.ptr(t), _lib.ptr(tri2cluster),
+              0 if tri2cluster is None else tri2cluster.shape[0], S, _lib.ptr(bitset), _lib.ptr(rast),
+              _lib.ptr(workspace) if want_rast else None, workspace.numel() if want_rast else 0, _lib.stream_of(p))
+    return rast, bitset
+
+
 def rasterize(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:
-    """``compute_fragments`` then ``depth_test`` (``rasterize.py:97-116``)."""
-    frag_pix, frag_attrs = compute_fragments(resolution, pos, tri)
-    return depth_test(pos.shape[0], resolution, frag_pix, frag_attrs)
+    """``compute_fragments`` then ``depth_test`` (``rasterize.py:97-116``), computed by the
+    fused single pass (the same rast as the two ops)."""
+    return rasterize_fused(resolution, pos, tri)[0]
 
 
 def barycentric_derivatives(rast: torch.Tensor, pos: torch.Tensor, tri: torch.Tensor) -> torch.Tensor:

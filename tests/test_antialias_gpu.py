@@ -66,6 +66,11 @@ def test_antialias_gradient(tag, kr, rho):
     assert float(loss.detach()) == 1.0
     (2.0 * loss).backward()
     got = np_(pos.grad) / 2.0
+    unfused = np_(s2c.antialiased_cluster_bitset_grad(*[cu(a[k]) for k in ("bitset", "target", "pos", "tri", "edges",
+                                                                            "edge2tri", "edge2cluster")],
+                                                       kernel_radius=kr, rho=rho, fused=False))
+    ok, err = grad_close(got, unfused, tol=1e-6)
+    assert ok, err
     ora = O.antialias_grad(a["bitset"], a["target"], a["pos"], a["tri"], a["edges"], a["edge2tri"], a["edge2cluster"],
                            kr, rho)
     ok, err = grad_close(got, ora)
@@ -109,12 +114,14 @@ def test_antialias_on_random_scene_matches_oracle():
     e2c = cards.tri2cluster[e2t[:, 0]].astype(np.int32)
     tgt = O.dda_cluster_bitset(H, W, sc.pos, sc.edges, sc.edge2cluster, K)
     bits = O.cluster_mask_from_fragments(H, W, *O.compute_fragments(H, W, cpos, cards.tri), cards.tri2cluster, K, B=2)
-    got = np_(s2c.antialiased_cluster_bitset_grad(cu(bits), cu(tgt), cu(cpos), cu(cards.tri), cu(edges), cu(e2t),
-                                                   cu(e2c), 7.0, 0.5))
     ora = O.antialias_grad(bits, tgt, cpos, cards.tri, edges, e2t, e2c, 7.0, 0.5)
-    ok, err = grad_close(got, ora)
-    assert ok, err
     assert np.abs(ora).max() > 0
+    for fused in (True, False):
+        got = np_(s2c.antialiased_cluster_bitset_grad(cu(bits), cu(tgt), cu(cpos), cu(cards.tri), cu(edges), cu(e2t),
+                                                       cu(e2c), 7.0, 0.5, fused=fused))
+        ok, err = grad_close(got, ora)
+        assert ok, (fused, err)
+        assert np.array_equal(got != 0, ora != 0)
 
 
 def test_xor_error_and_cluster_iou_exact():
@@ -132,3 +139,23 @@ def test_xor_error_and_cluster_iou_exact():
     bu = np.unpackbits(b.view(np.uint8), bitorder="little").reshape(-1, 96)[:, :K]
     assert np.array_equal(np_(inter), (au & bu).sum(0)) and np.array_equal(np_(uni), (au | bu).sum(0))
     assert np.array_equal(np_(iou), (au & bu).sum(0) / (au | bu).sum(0))
+
+
+@pytest.mark.parametrize("shape,K", [((1, 96_000_000 // 4096, 4096, 1), 1), ((1, 50, 80, 64), 2048),
+                                     ((2, 31, 17, 5), 150)])
+def test_cluster_iou_counts_large_and_ragged(shape, K):
+    """Per-thread runs longer than the 255-word flush period, many slots, a ragged K."""
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(K)
+    a = rng.integers(-2 ** 31, 2 ** 31 - 1, size=shape, dtype=np.int64).astype(np.int32)
+    b = a ^ (rng.integers(0, 2 ** 31 - 1, size=shape, dtype=np.int64).astype(np.int32) & 0x0f0f0f0f)
+    _, inter, uni = s2c.cluster_iou(cu(a), cu(b), K)
+    S = shape[-1]
+    ai = a.reshape(-1, S).view(np.uint32)
+    bi = b.reshape(-1, S).view(np.uint32)
+    ri, ru = np.zeros(K, np.int64), np.zeros(K, np.int64)
+    for c in range(K):
+        sl, bit = c // 32, np.uint32(1 << (c % 32))
+        x, y = (ai[:, sl] & bit) != 0, (bi[:, sl] & bit) != 0
+        ri[c], ru[c] = np.count_nonzero(x & y), np.count_nonzero(x | y)
+    assert np.array_equal(np_(inter), ri) and np.array_equal(np_(uni), ru)

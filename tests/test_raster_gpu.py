@@ -95,6 +95,10 @@ def test_fullsize_card_raster_matches_reference():
     orast = O.depth_test(1, 1024, 1024, ofp, ofa)
     assert np.array_equal(rast, orast)
     assert int((rast[..., 3] > 0).sum()) == ref["covered"]
+    # the fused single pass gives the same rast and bitset
+    frast, fbits = s2c.rasterize_fused((1024, 1024), cu(cpos), cu(cards.tri), cu(cards.tri2cluster), 2048)
+    assert hashlib.sha256(np_(fbits).tobytes()).hexdigest() == ref["bitset_sha256"]
+    assert np.array_equal(np_(frast), rast)
 
 
 def test_triangle_interpolation_forward_backward():
@@ -190,3 +194,46 @@ def test_barycentric_derivatives_perspective():
     tri = rng.integers(0, V, size=(T, 3)).astype(np.int32)
     rast, db = s2c.rasterize_with_derivatives((70, 90), cu(pos), cu(tri))
     assert close(np_(db), O.barycentric_derivatives(np_(rast), pos, tri))
+
+
+@pytest.mark.parametrize("name", ["tri_cards", "tri_random"])
+def test_rasterize_fused_matches_list_path(name):
+    import strns2cards_gb300 as s2c
+    d = golden(name + ".npz")
+    H, W = int(d["H"]), int(d["W"])
+    pos, tri = cu(d["pos"]), cu(d["tri"])
+    fp, fa = s2c.compute_fragments((H, W), pos, tri)
+    rast = s2c.depth_test(d["pos"].shape[0], (H, W), fp, fa)
+    t2c = cu(d["tri2cluster"]) if "tri2cluster" in d else torch.zeros(d["tri"].shape[0], dtype=torch.int32, device="cuda")
+    K = int(d["K"]) if "K" in d else 1
+    frast, fbits = s2c.rasterize_fused((H, W), pos, tri, t2c, K)
+    assert torch.equal(frast, rast)
+    B = d["pos"].shape[0]
+    ref_bits = torch.zeros((B, H, W, (K + 31) // 32), dtype=torch.int32, device="cuda")
+    from strns2cards_gb300 import _core
+    if fp.shape[0]:
+        _core.cluster_mask_from_fragments(fp, fa, t2c, ref_bits)
+    assert torch.equal(fbits, ref_bits)
+    # bitset only, rast only
+    r2, b2 = s2c.rasterize_fused((H, W), pos, tri, t2c, K, want_rast=False)
+    assert r2 is None and torch.equal(b2, ref_bits)
+
+
+def test_rasterize_fused_ties_and_perspective():
+    """Coincident triangles (exact depth ties: the lower triangle id wins, as the list path)
+    and perspective views with triangles behind the camera."""
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(31)
+    V, T, B = 200, 300, 3
+    pos = rng.uniform(-1.2, 1.2, size=(B, V, 4)).astype(np.float32)
+    pos[..., 3] = rng.uniform(-0.2, 1.5, size=(B, V))
+    pos[..., 2] *= np.abs(pos[..., 3]) * 0.7
+    tri = rng.integers(0, V, size=(T, 3)).astype(np.int32)
+    tri[T // 2:] = tri[:T - T // 2]                    # duplicates: exact ties
+    t2c = rng.integers(0, 40, size=T).astype(np.int32)
+    H, W = 64, 96
+    fr, fb = s2c.rasterize_fused((H, W), cu(pos), cu(tri), cu(t2c), 40)
+    orast = O.rasterize(H, W, pos, tri)
+    assert np.array_equal(np_(fr), orast)
+    ofp, ofa = O.compute_fragments(H, W, pos, tri)
+    assert np.array_equal(np_(fb), O.cluster_mask_from_fragments(H, W, ofp, ofa, t2c, 40, B=B))
