@@ -320,7 +320,9 @@ def wl_tri_raster(list_path=False):
     V, T, H = pos.shape[1], cards.tri.shape[0], 1024
 
     def setup(d):
-        return {"ws": torch.empty(8 * H * H + 256, dtype=torch.uint8, device=d["pos"].device),
+        from strns2cards_gb300 import _lib
+        need = _lib.lib().s2c_rasterize_fused_workspace_size(1, H, H, T)
+        return {"ws": torch.empty(need, dtype=torch.uint8, device=d["pos"].device),
                 "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=d["pos"].device),
                 "bits": torch.empty((1, H, H, 64), dtype=torch.int32, device=d["pos"].device)}
 
@@ -397,7 +399,9 @@ def wl_iteration():
         dev = d["pos"].device
         tgt = s2c.dda_cluster_bitset((H, H), torch.from_numpy(spos).to(dev), torch.from_numpy(sedges).to(dev),
                                      torch.from_numpy(se2c).to(dev), 2048)
-        return {"tgt": tgt, "ws": torch.empty(8 * H * H + 256, dtype=torch.uint8, device=dev),
+        from strns2cards_gb300 import _lib
+        need = _lib.lib().s2c_rasterize_fused_workspace_size(1, H, H, T)
+        return {"tgt": tgt, "ws": torch.empty(need, dtype=torch.uint8, device=dev),
                 "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=dev),
                 "bits": torch.empty((1, H, H, 64), dtype=torch.int32, device=dev)}
 

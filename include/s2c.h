@@ -152,9 +152,10 @@ S2C_API s2c_status s2c_depth_test(int B, int H, int W, int64_t num_frags, const 
  * fragment list or host synchronisation (capturable in a CUDA graph).  rast (B, H, W, 4)
  * (nullable) equals depth_test's output (exact depth ties go to the lower triangle id);
  * bitset (B, H, W, S) (nullable; zeroed here) equals cluster_mask_from_fragments' for
- * tri2cluster (num_tri2cluster entries).  The workspace holds B*H*W 64-bit depth keys
- * (needed only with rast). */
-S2C_API size_t s2c_rasterize_fused_workspace_size(int B, int H, int W);
+ * tri2cluster (num_tri2cluster entries).  The workspace holds the B*H*W 64-bit depth
+ * keys, the triangles' screen rectangles and the prefix of their areas (the work is split
+ * evenly over the bbox pixels on the device). */
+S2C_API size_t s2c_rasterize_fused_workspace_size(int B, int H, int W, int T);
 S2C_API s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream);

@@ -151,19 +151,35 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
     const float cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
     const float alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
     const float kr2 = __fmul_rn(A.kr, A.kr);
-    double acc = 0.0;
-    for (int j = lane; j < taps; j += 32) {
-        const int th = h0 + j / ww, tw = w0 + j % ww;
-        const int64_t pix = img + (int64_t)th * A.W + tw;
-        const int c0 = bit_of(A.bitset, pix, A.S, c), c1 = bit_of(A.target, pix, A.S, c);
-        if (c0 == c1) continue;
-        const float dx = __fsub_rn(__fadd_rn((float)tw, 0.5f), fx);
-        const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), fy);
-        const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-        if (!(n2 < kr2)) continue;
-        const double wgt = (double)cc * (double)expf(-alpha * n2);
-        acc += wgt * (double)(c0 - c1) * (c1 == 0 ? (double)A.rho : 1.0);
+    // each lane sums its taps (at most ceil(taps / 32) of them) in FP32; the lanes' partial
+    // sums are reduced in FP64.  Tap j = lane + 32 i sits at (row, col) = divmod(j, ww),
+    // stepped incrementally.
+    float part = 0.f;
+    if (taps > 0) {
+        const int s_row = 32 / ww, s_col = 32 - s_row * ww;
+        int row = lane / ww, col = lane - (lane / ww) * ww;
+        const int slot = c >> 5, bit = c & 31;
+        for (int j = lane; j < taps; j += 32) {
+            const int th = h0 + row, tw = w0 + col;
+            const int64_t pix = (img + (int64_t)th * A.W + tw) * A.S + slot;
+            const int c0 = (__ldg(A.bitset + pix) >> bit) & 1, c1 = (__ldg(A.target + pix) >> bit) & 1;
+            row += s_row;
+            col += s_col;
+            if (col >= ww) {
+                col -= ww;
+                ++row;
+            }
+            if (c0 == c1) continue;
+            const float dx = __fsub_rn(__fadd_rn((float)tw, 0.5f), fx);
+            const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), fy);
+            const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+            if (!(n2 < kr2)) continue;
+            const float wgt = __fmul_rn(cc, expf(-alpha * n2));
+            const float sgn = c0 ? (c1 ? 0.f : A.rho) : -1.f;   // (c0 - c1) * (c1 == 0 ? rho : 1)
+            part = __fmaf_rn(wgt, sgn, part);
+        }
     }
+    double acc = (double)part;
 #pragma unroll
     for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
     o.dc = (double)c01 * acc;
@@ -266,6 +282,7 @@ __global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
             if (!z_ok(dda_z(p0, p1, t1))) continue;
             AAFrag f;
             if (!aa_fragment(A, b, h, w, sp.axis, t1, ee, nrm, lane, f)) continue;
+            if (lane != 0) continue;
             double qx, qy, qw;
             if (!aa_chain64(A, f, qx, qy, qw)) continue;
             s0x += qx * (double)f.t0;

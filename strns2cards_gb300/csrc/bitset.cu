@@ -81,8 +81,8 @@ __global__ void __launch_bounds__(256) xor_popcount_kernel(int64_t nwords, const
 // Per-cluster pixel counts of a & b and a | b.  Each thread keeps one slot s for its whole
 // run (its word stride is a multiple of S), so the 32 clusters of that slot are counted
 // positionally in registers: 4-bit counters per bit (x >> r) & 0x11111111 for r = 0..3,
-// spread into 8-bit counters every 15 words, and those added to the block's per-cluster
-// counters every 255 words; the block's counters go to the global uint64 totals once.
+// spread into 8-bit counters every 12 words, and those added to the block's per-cluster
+// counters every 252 words; the block's counters go to the global uint64 totals once.
 __device__ __forceinline__ void iou_nib_flush(uint32_t* n, uint32_t* b) {
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -127,20 +127,31 @@ __global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, i
         const int base = (int)(t % S) * 32;
         uint32_t nI[4] = {0u, 0u, 0u, 0u}, nU[4] = {0u, 0u, 0u, 0u};
         uint32_t bI[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u}, bU[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        // four independent words per step (loads in flight); nibbles hold 12 words, bytes
+        // 21 nibble flushes (252 words)
         int cn = 0, cb = 0;
-        for (int64_t i = t; i < nwords; i += tstride) {
-            const uint32_t x = (uint32_t)__ldcs(a + i), y = (uint32_t)__ldcs(b + i);
-            const uint32_t ia = x & y, ua = x | y;
+        for (int64_t i = t; i < nwords; i += 4 * tstride) {
+            uint32_t xs[4], ys[4];
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                nI[r] += (ia >> r) & 0x11111111u;
-                nU[r] += (ua >> r) & 0x11111111u;
+            for (int u = 0; u < 4; ++u) {
+                const int64_t k = i + u * tstride;
+                xs[u] = k < nwords ? (uint32_t)__ldcs(a + k) : 0u;
+                ys[u] = k < nwords ? (uint32_t)__ldcs(b + k) : 0u;
             }
-            if (++cn == 15) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const uint32_t ia = xs[u] & ys[u], ua = xs[u] | ys[u];
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    nI[r] += (ia >> r) & 0x11111111u;
+                    nU[r] += (ua >> r) & 0x11111111u;
+                }
+            }
+            if (++cn == 3) {
                 cn = 0;
                 iou_nib_flush(nI, bI);
                 iou_nib_flush(nU, bU);
-                if (++cb == 17) {
+                if (++cb == 21) {
                     cb = 0;
                     iou_byte_flush(bI, use_smem ? hist : nullptr, inter, base, K);
                     iou_byte_flush(bU, use_smem ? hist + K : nullptr, uni, base, K);

@@ -61,31 +61,62 @@ __global__ void __launch_bounds__(256) tri_rects_kernel(int H, int W, int B, Tri
     counts[idx] = (int32_t)((uint32_t)rc.y * (uint32_t)rc.w);
 }
 
-// Coverage of pixel (x, y) by a triangle with clip-space corners P0..P2
-// (rasterize.cu:132-163).  Returns true and (b0, b1, z) when covered.
-__device__ __forceinline__ bool tri_cover(int H, int W, float4 P0, float4 P1, float4 P2, int x, int y, float& b0,
-                                          float& b1, float& z) {
-    const float px = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)x, 0.5f)), (float)W));
-    const float py = __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)y, 0.5f)), (float)H));
+// Pixel centre in NDC (rasterize.cu:132-133)
+__device__ __forceinline__ float ndc_of(int i, float n) {
+    return __fadd_rn(-1.f, __fdiv_rn(__fmul_rn(2.f, __fadd_rn((float)i, 0.5f)), n));
+}
+
+// Clip-space edge functions of a pixel centre (rasterize.cu:140-150)
+struct TriEdges {
+    float A0, A1, A2, A;
+};
+
+__device__ __forceinline__ TriEdges tri_edges(float4 P0, float4 P1, float4 P2, float px, float py) {
     const float q0x = __fmaf_rn(-px, P0.w, P0.x), q0y = __fmaf_rn(-py, P0.w, -P0.y);
     const float q1x = __fmaf_rn(-px, P1.w, P1.x), q1y = __fmaf_rn(-py, P1.w, -P1.y);
     const float q2x = __fmaf_rn(-px, P2.w, P2.x), q2y = __fmaf_rn(-py, P2.w, -P2.y);
+    TriEdges e;
     // a*b - c*d is fused on its first product
-    const float A0 = __fmaf_rn(q1x, q2y, -__fmul_rn(q1y, q2x));
-    const float A1 = __fmaf_rn(q2x, q0y, -__fmul_rn(q2y, q0x));
-    const float A2 = __fmaf_rn(q0x, q1y, -__fmul_rn(q0y, q1x));
-    const float A = __fadd_rn(__fadd_rn(A0, A1), A2);
-    if (A == 0.f) return false;
-    const float invA = __fdiv_rn(1.f, A);
-    b0 = __fmul_rn(A0, invA);
-    b1 = __fmul_rn(A1, invA);
+    e.A0 = __fmaf_rn(q1x, q2y, -__fmul_rn(q1y, q2x));
+    e.A1 = __fmaf_rn(q2x, q0y, -__fmul_rn(q2y, q0x));
+    e.A2 = __fmaf_rn(q0x, q1y, -__fmul_rn(q0y, q1x));
+    e.A = __fadd_rn(__fadd_rn(e.A0, e.A1), e.A2);
+    return e;
+}
+
+// rasterize.cu:151-163: barycentrics, depth and the acceptance test
+__device__ __forceinline__ bool tri_finish(const TriEdges& e, float4 P0, float4 P1, float4 P2, float& b0, float& b1,
+                                           float& z) {
+    if (e.A == 0.f) return false;
+    const float invA = __fdiv_rn(1.f, e.A);
+    b0 = __fmul_rn(e.A0, invA);
+    b1 = __fmul_rn(e.A1, invA);
     // (A0 z0 + A1 z1) + A2 z2 and the same for w, with the reference build's fusion shapes
-    const float zc = __fmaf_rn(A2, P2.z, __fmaf_rn(A1, P1.z, __fmul_rn(A0, P0.z)));
-    const float wc = __fmaf_rn(A2, P2.w, __fmaf_rn(A0, P0.w, __fmul_rn(A1, P1.w)));
+    const float zc = __fmaf_rn(e.A2, P2.z, __fmaf_rn(e.A1, P1.z, __fmul_rn(e.A0, P0.z)));
+    const float wc = __fmaf_rn(e.A2, P2.w, __fmaf_rn(e.A0, P0.w, __fmul_rn(e.A1, P1.w)));
     z = __fdiv_rn(zc, wc);
     if (!isfinite(b0) || !isfinite(b1) || !isfinite(z)) return false;
     if (b0 < 0.f || b1 < 0.f || __fadd_rn(b0, b1) > 1.f || z < -1.f || z > 1.f) return false;
     return true;
+}
+
+// Coverage of pixel (x, y) by a triangle with clip-space corners P0..P2
+// (rasterize.cu:132-163).  Returns true and (b0, b1, z) when covered.
+__device__ __forceinline__ bool tri_cover(int H, int W, float4 P0, float4 P1, float4 P2, int x, int y, float& b0,
+                                          float& b1, float& z) {
+    const TriEdges e = tri_edges(P0, P1, P2, ndc_of(x, (float)W), ndc_of(y, (float)H));
+    return tri_finish(e, P0, P1, P2, b0, b1, z);
+}
+
+// Exact early rejection: with A and A_i finite, opposite signs and |A_i| > 1e-30 |A|, the
+// product A_i * fl(1 / A) is a nonzero number of A_i's sign * sign(A) (no underflow), so
+// b_i < 0 and tri_finish rejects the pixel.
+__device__ __forceinline__ bool tri_surely_outside(const TriEdges& e) {
+    if (!isfinite(e.A) || e.A == 0.f) return e.A == 0.f;
+    const float lim = __fmul_rn(fabsf(e.A), 1e-30f);
+    const bool out0 = isfinite(e.A0) && e.A0 != 0.f && ((e.A0 < 0.f) != (e.A < 0.f)) && fabsf(e.A0) > lim;
+    const bool out1 = isfinite(e.A1) && e.A1 != 0.f && ((e.A1 < 0.f) != (e.A < 0.f)) && fabsf(e.A1) > lim;
+    return out0 || out1;
 }
 
 // rasterize.cu:90-172: one thread per bounding-box pixel, owner triangle by binary search
@@ -159,74 +190,163 @@ __global__ void __launch_bounds__(256) depth_gather_kernel(int64_t npix, const u
 }
 
 // Fused raster (compute_fragments + depth_test + cluster_mask_from_fragments without the
-// fragment list): each warp takes 32 triangles and spreads the pixels of their screen
-// rectangles over its lanes (owner found by a shuffle binary search over the warp's
-// inclusive prefix of rectangle areas).  A covered pixel ORs its cluster bit into the
-// bitset and offers the key (bits(z + 2) << 32 | t) to the pixel's 64-bit minimum:
-// within one pixel the list path's fragment order is triangle order, so the minimum
-// picks the fragment the list-based depth test picks.
+// fragment list).  A covered pixel ORs its cluster bit into the bitset and offers the key
+// (bits(z + 2) << 32 | t) to the pixel's 64-bit minimum: within one pixel the list path's
+// fragment order is triangle order, so the minimum picks the fragment the list-based
+// depth test picks.
 struct FusedRaster {
     int B, H, W, S;
     Tris R;
-    const int32_t* __restrict__ t2c;      // nullable
+    const int32_t* __restrict__ t2c;        // nullable
     int num_t2c;
-    int32_t* __restrict__ bitset;         // nullable
+    int32_t* __restrict__ bitset;           // nullable
     unsigned long long* __restrict__ keys;  // nullable
+    const int4* __restrict__ rects;         // (B*T) screen rectangles
+    const uint32_t* __restrict__ prefix;    // (B*T) inclusive prefix of their areas
+    const int64_t* __restrict__ total;      // device: sum of the areas
 };
 
+__device__ __forceinline__ void raster_pixel(const FusedRaster& F, const float* px_lut, const float* py_lut, int ob,
+                                             int ot, int x, int y) {
+    if (x < 0 || x >= F.W || y < 0 || y >= F.H) return;
+    const int i0 = __ldg(F.R.tri + 3 * ot), i1 = __ldg(F.R.tri + 3 * ot + 1), i2 = __ldg(F.R.tri + 3 * ot + 2);
+    if ((unsigned)i0 >= (unsigned)F.R.V || (unsigned)i1 >= (unsigned)F.R.V || (unsigned)i2 >= (unsigned)F.R.V) return;
+    const float4* pb = F.R.pos4 + (int64_t)ob * F.R.V;
+    const float4 P0 = __ldg(pb + i0), P1 = __ldg(pb + i1), P2 = __ldg(pb + i2);
+    const float px = px_lut ? px_lut[x] : ndc_of(x, (float)F.W);
+    const float py = py_lut ? py_lut[y] : ndc_of(y, (float)F.H);
+    const TriEdges e = tri_edges(P0, P1, P2, px, py);
+    if (tri_surely_outside(e)) return;
+    float b0, b1, z;
+    if (!tri_finish(e, P0, P1, P2, b0, b1, z)) return;
+    const int64_t pix = ((int64_t)ob * F.H + y) * F.W + x;
+    if (F.keys) {
+        const float zz = __fadd_rn(z, 2.f);
+        atomicMin(F.keys + pix, ((unsigned long long)(uint32_t)__float_as_int(zz) << 32) | (uint32_t)ot);
+    }
+    if (F.bitset && ot < F.num_t2c) {
+        const int c = __ldg(F.t2c + ot);
+        if (c >= 0 && c < 32 * F.S) atomicOr(F.bitset + pix * F.S + (c >> 5), (int32_t)(1u << (c & 31)));
+    }
+}
+
+// local / w for 0 <= local, 1 <= w: float estimate corrected by one step (exact while
+// local < 2^22), integer division beyond
+__device__ __forceinline__ int divmod_small(int local, int w, int& r) {
+    int q;
+    if (local < (1 << 22)) {
+        q = __float2int_rz(__fmul_rn(__int2float_rn(local), __frcp_rn((float)w)));
+        r = local - q * w;
+        if (r < 0) { --q; r += w; }
+        else if (r >= w) { ++q; r -= w; }
+    } else {
+        q = local / w;
+        r = local - q * w;
+    }
+    return q;
+}
+
+constexpr int kRasterChunk = 1024;
+
+// Balanced pass: warps take equal chunks of the global bbox-pixel index space.  A warp
+// keeps a window of 32 consecutive triangles' prefix values in its lanes, slides it along
+// the chunk, and each lane finds the owner of its pixel with a 5-step shuffle search.
 __global__ void __launch_bounds__(256) tri_fused_kernel(FusedRaster F) {
+    extern __shared__ float lut[];
+    const bool use_lut = F.W + F.H <= 8192;
+    if (use_lut) {
+        for (int i = threadIdx.x; i < F.W; i += blockDim.x) lut[i] = ndc_of(i, (float)F.W);
+        for (int i = threadIdx.x; i < F.H; i += blockDim.x) lut[F.W + i] = ndc_of(i, (float)F.H);
+        __syncthreads();
+    }
+    const float* px_lut = use_lut ? lut : nullptr;
+    const float* py_lut = use_lut ? lut + F.W : nullptr;
     const int lane = threadIdx.x & 31;
     const int64_t BT = (int64_t)F.B * F.R.T;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    for (int64_t g = warp0 * 32; g < BT; g += nwarps * 32) {
-        const int64_t mine = g + lane;
-        int4 rc = make_int4(0, 0, 0, 0);
-        int b = 0, t = 0;
-        if (mine < BT) {
-            b = (int)F.R.divT.div((uint32_t)mine);
-            t = (int)mine - b * F.R.T;
-            rc = tri_rect(F.H, F.W, F.R, b, t);
+    const int64_t total = *F.total;
+    if (total > 0xffffffffLL) {
+        // areas beyond 32 bits: each warp walks 32 whole triangles (correct, unbalanced)
+        for (int64_t g = warp0 * 32; g < BT; g += nwarps * 32) {
+            const int64_t mine = g + lane;
+            int4 rc = make_int4(0, 0, 0, 0);
+            int b = 0, t = 0;
+            if (mine < BT) {
+                b = (int)F.R.divT.div((uint32_t)mine);
+                t = (int)mine - b * F.R.T;
+                rc = F.rects[mine];
+            }
+            for (int k = 0; k < rc.y * rc.w; ++k) {
+                int r;
+                const int q = divmod_small(k, rc.w, r);
+                raster_pixel(F, px_lut, py_lut, b, t, rc.z + r, rc.x + q);
+            }
         }
-        // inclusive prefix of the areas over the warp (areas < 2^31 since H, W <= 32768)
-        int64_t pre = (int64_t)rc.y * rc.w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int64_t v = __shfl_up_sync(0xffffffffu, pre, o);
-            if (lane >= o) pre += v;
+        return;
+    }
+    const uint32_t tot = (uint32_t)total;
+    const int64_t nchunks = ((int64_t)tot + kRasterChunk - 1) / kRasterChunk;
+    for (int64_t ch = warp0; ch < nchunks; ch += nwarps) {
+        const uint32_t c0 = (uint32_t)(ch * kRasterChunk);
+        const uint32_t c1 = (uint32_t)min((int64_t)tot, (ch + 1) * kRasterChunk);
+        // first triangle whose inclusive prefix exceeds c0 (same search on every lane)
+        int64_t lo = 0, hi = BT;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if (__ldg(F.prefix + mid) <= c0) lo = mid + 1;
+            else hi = mid;
         }
-        const int64_t total = __shfl_sync(0xffffffffu, pre, 31);
-        for (int64_t base = 0; base < total; base += 32) {
-            const int64_t j = base + lane;
-            // owner: first lane whose inclusive prefix exceeds j
-            int lo = 0;
+        int64_t t0 = lo;
+        uint32_t start = t0 > 0 ? __ldg(F.prefix + t0 - 1) : 0u;
+        uint32_t pre = t0 + lane < BT ? __ldg(F.prefix + t0 + lane) : 0xffffffffu;
+        uint32_t base = c0;
+        while (base < c1) {
+            // slide the window until its first triangle holds `base`
+            for (;;) {
+                const unsigned m = __ballot_sync(0xffffffffu, pre <= base);
+                if (!m) break;
+                const int adv = __popc(m);
+                start = __shfl_sync(0xffffffffu, pre, adv - 1);
+                t0 += adv;
+                pre = t0 + lane < BT ? __ldg(F.prefix + t0 + lane) : 0xffffffffu;
+            }
+            const uint32_t wend = __shfl_sync(0xffffffffu, pre, 31);
+            const uint32_t end = min(min(c1, base + 32u), wend);
+            const uint32_t j = base + lane;
+            int ow = 0;
 #pragma unroll
             for (int step = 16; step; step >>= 1) {
-                const int64_t pv = __shfl_sync(0xffffffffu, pre, lo + step - 1);
-                if (pv <= j) lo += step;
+                const uint32_t pv = __shfl_sync(0xffffffffu, pre, ow + step - 1);
+                if (pv <= j) ow += step;
             }
-            const int64_t pv_prev = __shfl_sync(0xffffffffu, pre, lo > 0 ? lo - 1 : 0);
-            const int ob = __shfl_sync(0xffffffffu, b, lo), ot = __shfl_sync(0xffffffffu, t, lo);
-            const int rh0 = __shfl_sync(0xffffffffu, rc.x, lo), rw0 = __shfl_sync(0xffffffffu, rc.z, lo);
-            const int rwl = __shfl_sync(0xffffffffu, rc.w, lo);
-            if (j >= total) continue;
-            const int local = (int)(j - (lo > 0 ? pv_prev : 0));
-            const int y = rh0 + local / rwl, x = rw0 + local % rwl;
-            if (x < 0 || x >= F.W || y < 0 || y >= F.H) continue;
-            const int i0 = __ldg(F.R.tri + 3 * ot), i1 = __ldg(F.R.tri + 3 * ot + 1), i2 = __ldg(F.R.tri + 3 * ot + 2);
-            const float4* pb = F.R.pos4 + (int64_t)ob * F.R.V;
-            float b0, b1, z;
-            if (!tri_cover(F.H, F.W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z)) continue;
-            const int64_t pix = ((int64_t)ob * F.H + y) * F.W + x;
-            if (F.keys) {
-                const float zz = __fadd_rn(z, 2.f);
-                atomicMin(F.keys + pix, ((unsigned long long)(uint32_t)__float_as_int(zz) << 32) | (uint32_t)ot);
+            const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
+            if (j < end) {
+                const int64_t o = t0 + ow;
+                const int ob = (int)F.R.divT.div((uint32_t)o);
+                const int ot = (int)o - ob * F.R.T;
+                const int4 rc = F.rects[o];
+                const int local = (int)(j - (ow > 0 ? prev : start));
+                int r;
+                const int q = divmod_small(local, rc.w, r);
+                raster_pixel(F, px_lut, py_lut, ob, ot, rc.z + r, rc.x + q);
             }
-            if (F.bitset && ot < F.num_t2c) {
-                const int c = __ldg(F.t2c + ot);
-                if (c >= 0 && c < 32 * F.S) atomicOr(F.bitset + pix * F.S + (c >> 5), (int32_t)(1u << (c & 31)));
-            }
+            base = end;
         }
+    }
+}
+
+// screen rectangle and area of every (view, triangle)
+__global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B, Tris R, int4* __restrict__ rects,
+                                                            int32_t* __restrict__ areas) {
+    const int64_t n = (int64_t)B * R.T;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)R.divT.div((uint32_t)idx);
+        const int t = (int)idx - b * R.T;
+        const int4 rc = tri_rect(H, W, R, b, t);
+        rects[idx] = rc;
+        areas[idx] = (int32_t)((uint32_t)rc.y * (uint32_t)rc.w);
     }
 }
 
@@ -545,8 +665,34 @@ extern "C" s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int 
     return S2C_OK;
 }
 
-extern "C" size_t s2c_rasterize_fused_workspace_size(int B, int H, int W) {
-    return (size_t)(B > 0 ? B : 0) * (size_t)(H > 0 ? H : 0) * (size_t)(W > 0 ? W : 0) * 8 + 256;
+namespace {
+struct RasterWs {
+    unsigned long long* keys;
+    int4* rects;
+    int32_t* areas;
+    int32_t* prefix;
+    int64_t* total;
+    void* scan;
+};
+
+size_t raster_carve(int B, int H, int W, int T, bool with_keys, void* base, size_t cap, RasterWs* w) {
+    Carver cv(base, cap);
+    RasterWs r;
+    const int64_t BT = std::max<int64_t>((int64_t)B * T, 1);
+    r.keys = with_keys ? cv.take<unsigned long long>((size_t)B * H * W) : nullptr;
+    r.rects = cv.take<int4>(BT);
+    r.areas = cv.take<int32_t>(BT);
+    r.prefix = cv.take<int32_t>(BT);
+    r.total = cv.take<int64_t>(1);
+    r.scan = cv.take<char>(scan_workspace_bytes(BT));
+    if (w) *w = r;
+    return cv.off;
+}
+}  // namespace
+
+extern "C" size_t s2c_rasterize_fused_workspace_size(int B, int H, int W, int T) {
+    if (B <= 0 || H <= 0 || W <= 0 || T < 0) return 256;
+    return raster_carve(B, H, W, T, true, nullptr, (size_t)-1, nullptr) + 256;
 }
 
 extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
@@ -560,12 +706,12 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
     S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && (!rast || ((uintptr_t)rast & 15) == 0), "rasterize_fused: misaligned");
     const int64_t npix = (int64_t)B * H * W;
     cudaStream_t st = (cudaStream_t)stream;
-    unsigned long long* keys = nullptr;
+    RasterWs ws;
+    const size_t need = raster_carve(B, H, W, T, rast != nullptr, workspace, workspace_bytes, &ws);
+    S2C_REQUIRE(workspace && need <= workspace_bytes, "rasterize_fused: workspace of %zu bytes, need %zu",
+                workspace_bytes, need);
     if (rast) {
-        S2C_REQUIRE(workspace && workspace_bytes >= (size_t)npix * 8 && ((uintptr_t)workspace & 7) == 0,
-                    "rasterize_fused: workspace of %zu bytes, need %lld", workspace_bytes, (long long)(npix * 8));
-        keys = (unsigned long long*)workspace;
-        cudaError_t e = cudaMemsetAsync(keys, 0xff, (size_t)npix * 8, st);
+        cudaError_t e = cudaMemsetAsync(ws.keys, 0xff, (size_t)npix * 8, st);
         if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset keys");
     }
     if (bitset) {
@@ -580,6 +726,11 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
     R.divT = FastDiv((uint32_t)(T > 0 ? T : 1));
     const int64_t BT = (int64_t)B * T;
     if (BT > 0 && (rast || bitset)) {
+        tri_rect_area_kernel<<<grid_for(BT, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(H, W, B, R, ws.rects,
+                                                                                           ws.areas);
+        S2C_CHECK_LAUNCH("tri_rect_area_kernel");
+        s2c_status s = inclusive_scan_i32(ws.areas, BT, ws.prefix, ws.scan, ws.total, st);
+        if (s != S2C_OK) return s;
         FusedRaster F;
         F.B = B;
         F.H = H;
@@ -589,13 +740,16 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
         F.t2c = tri2cluster;
         F.num_t2c = num_tri2cluster;
         F.bitset = bitset;
-        F.keys = keys;
-        const int64_t warps = std::min<int64_t>((BT + 31) / 32, (int64_t)num_sms() * 64);
-        tri_fused_kernel<<<grid_for(warps * 32, 256), 256, 0, st>>>(F);
+        F.keys = ws.keys;
+        F.rects = ws.rects;
+        F.prefix = (const uint32_t*)ws.prefix;
+        F.total = ws.total;
+        const size_t lut = W + H <= 8192 ? (size_t)(W + H) * sizeof(float) : 0;
+        tri_fused_kernel<<<(unsigned)num_sms() * 8, 256, lut, st>>>(F);
         S2C_CHECK_LAUNCH("tri_fused_kernel");
     }
     if (rast) {
-        tri_resolve_kernel<<<grid_for(npix, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(B, H, W, R, keys,
+        tri_resolve_kernel<<<grid_for(npix, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(B, H, W, R, ws.keys,
                                                                                            (float4*)rast);
         S2C_CHECK_LAUNCH("tri_resolve_kernel");
     }

@@ -91,12 +91,12 @@ def rasterize_fused(resolution: Tuple[int, int], pos: torch.Tensor, tri: torch.T
         rast = torch.empty((B, H, W, 4), dtype=torch.float32, device=dev)
     if not want_rast:
         rast = None
-    need = _lib.lib().s2c_rasterize_fused_workspace_size(B, H, W) if want_rast else 0
-    if want_rast and (workspace is None or workspace.numel() < need):
+    need = _lib.lib().s2c_rasterize_fused_workspace_size(B, H, W, t.shape[0])
+    if workspace is None or workspace.numel() < need:
         workspace = _lib.workspace(need, dev)
     _lib.call("s2c_rasterize_fused", B, H, W, V, _lib.ptr(p), t.shape[0], _lib.ptr(t), _lib.ptr(tri2cluster),
               0 if tri2cluster is None else tri2cluster.shape[0], S, _lib.ptr(bitset), _lib.ptr(rast),
-              _lib.ptr(workspace) if want_rast else None, workspace.numel() if want_rast else 0, _lib.stream_of(p))
+              _lib.ptr(workspace), workspace.numel(), _lib.stream_of(p))
     return rast, bitset
 
 
