@@ -524,6 +524,79 @@ def wl_laplacian():
                 workload="10 Jacobi Laplacian steps (lambda 0.5) on 4,096 cards of 32x4 quads (165 vertices each)")
 
 
+def run_batched_fit(args):
+    """Batched cluster fit: 256 clusters (log-uniform 20..2000 strands x 64 vertices, seed 0),
+    local 128 x 512 frames, K = 1, one 32 x 4-quad card each; an iteration = coverage + card
+    raster + antialias backward + 10 Laplacian steps.  Metric: cluster-fit iterations per
+    second of the autotuned batched schedule; the per-cluster call sequence is timed beside."""
+    import torch
+    from strns2cards_gb300.batched import BatchedClusterFit, FitSchedule, synthetic_clusters
+    batch = synthetic_clusters()
+    C = batch.card_pos.shape[0]
+    fit = BatchedClusterFit(batch)
+    sched = FitSchedule(fit, trials=3)
+    for _ in range(max(args.warmup, 3)):
+        fit.step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        a.record(stream)
+        for _ in range(args.steps):
+            fit.step()
+        b.record(stream)
+        torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3
+    value = C * args.steps / t
+    # the per-cluster call sequence (the reference's way of fitting), a few iterations
+    plain = BatchedClusterFit(batch)
+    plain.prepare_plain()
+    plain.plain_iteration()
+    torch.cuda.synchronize()
+    k = 2
+    a.record(stream)
+    for _ in range(k):
+        plain.plain_iteration()
+    b.record(stream)
+    torch.cuda.synchronize()
+    plain_rate = C * k / (a.elapsed_time(b) / 1e3)
+    # end to end: card and strand positions in from pinned host memory, cards out
+    sp = torch.from_numpy(batch.strand_pos).pin_memory()
+    cp = torch.from_numpy(batch.card_pos).pin_memory()
+    out = torch.empty(cp.shape, dtype=torch.float32).pin_memory()
+    fit.mode = "graph" if sched.best.startswith("graph") else sched.best
+    if fit.mode == "graph":
+        fit.capture(two_streams=sched.best == "graph2")
+
+    def e2e_step():
+        fit.spos.copy_(sp, non_blocking=True)
+        fit.cpos.copy_(cp, non_blocking=True)
+        fit.step()
+        out.copy_(fit.cpos, non_blocking=True)
+    e2e_step()
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(3):
+        e2e_step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    e2e = C * 3 / (a.elapsed_time(b) / 1e3)
+    line = {"metric": "cluster-fit iterations per second (batched, autotuned schedule)", "value": value,
+            "unit": "cluster-iter/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{C} clusters (log-uniform 20..2000 strands x 64 verts, seed 0), 128x512 local "
+                                   "frames, K=1, one 32x4-quad card each; iteration = fused DDA coverage + fused "
+                                   "card raster + fused antialias backward + gradient step + 10 Laplacian steps",
+                       "schedule": sched.best, "schedule_ms": sched.results,
+                       "plain_per_cluster_calls": {"value": plain_rate, "unit": "cluster-iter/s"},
+                       "batched_over_plain": value / plain_rate, "strand_segments": int(batch.edge_ids.shape[0])},
+            "e2e": {"value": e2e, "unit": "cluster-iter/s", "h2d_bytes_per_step": sp.nbytes + cp.nbytes,
+                    "d2h_bytes_per_step": out.nbytes},
+            "roofline": None, "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": None}
+    print(json.dumps(line), flush=True)
+
+
 WORKLOADS = {"tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
              "cluster_iou": wl_cluster_iou,
@@ -602,11 +675,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["dda_bitset"] + sorted(WORKLOADS), default="dda_bitset",
+    ap.add_argument("--workload", choices=["dda_bitset", "batched_fit"] + sorted(WORKLOADS), default="dda_bitset",
                     help="dda_bitset (default) is the headline; the others time the remaining rows")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched_fit":
+        run_batched_fit(args)
     elif args.workload != "dda_bitset":
         run_workload(args)
     else:

@@ -209,6 +209,13 @@ S2C_API s2c_status s2c_compact_valid_ints(int64_t n, const int32_t* input, int32
  * bitset utilities                                                                    *
  * ---------------------------------------------------------------------------------- */
 
+/* new: cluster planes of a bitset: planes (B, 32 S, H, ceil(W / 32)) uint32, bit (x & 31) of
+ * word x >> 5 in row y of plane c = bit c of pixel (y, x).  A window of one cluster is then
+ * a few contiguous words per row instead of one 32-byte sector per pixel. */
+S2C_API size_t s2c_bitset_planes_size(int B, int H, int W, int S);
+S2C_API s2c_status s2c_bitset_to_planes(int B, int H, int W, int S, const int32_t* bitset, uint32_t* planes,
+                                        s2c_stream stream);
+
 /* replaces: popcount_bitset (pystrns2cards.cpp:507-529; bitset_utils.cu:37-52,392-404) */
 S2C_API s2c_status s2c_popcount_bitset(int64_t num_pixels, int S, const int32_t* bitset,
                                float* count_image, s2c_stream stream);
@@ -264,12 +271,22 @@ S2C_API s2c_status s2c_backward_antialiased_cluster_bitset_f64(
  * DDA walk of each marked edge and every fragment's window, fused per (view, edge), with no
  * fragment list and no host synchronisation (capturable in a CUDA graph).  Same
  * contributions as mark_discontinuity_edges + dda_compute_fragments + the backward above;
- * d_pos (B, V, 4) accumulated via the FP64 workspace (B*V*3 doubles). */
-S2C_API size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V);
+ * d_pos (B, V, 4) accumulated.  The workspace holds the FP64 accumulator (B*V*3 doubles)
+ * and the cluster planes of both bitsets (see s2c_bitset_to_planes), read by the windows. */
+S2C_API size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S);
 S2C_API s2c_status s2c_antialiased_cluster_bitset_grad(
     int B, int H, int W, int S, const int32_t* bitset, const int32_t* target, int V, const float* pos, int T,
     const int32_t* tri, int E, const int32_t* edges, const int32_t* edge2tri, const int32_t* edge2cluster,
     float* d_pos, float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream);
+
+/* new: the same from cluster planes the caller keeps (e.g. the target's, built once per fit);
+ * workspace: B*V*3 doubles. */
+S2C_API size_t s2c_antialiased_cluster_bitset_grad_planes_workspace_size(int B, int V);
+S2C_API s2c_status s2c_antialiased_cluster_bitset_grad_planes(
+    int B, int H, int W, int S, const uint32_t* bitset_planes, const uint32_t* target_planes, int V,
+    const float* pos, int T, const int32_t* tri, int E, const int32_t* edges, const int32_t* edge2tri,
+    const int32_t* edge2cluster, float* d_pos, float kernel_radius, float rho, void* workspace,
+    size_t workspace_bytes, s2c_stream stream);
 
 /* ---------------------------------------------------------------------------------- *
  * strand curves                                                                       *

@@ -332,7 +332,7 @@ def antialiased_cluster_bitset_grad(bitset, target_bitset, pos, tri, edges, edge
     V = pos.shape[1]
     if d_pos is None:
         d_pos = torch.zeros_like(pos)
-    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_workspace_size(B, V)
+    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S)
     if ws is None or ws.numel() < need:
         ws = workspace(need, pos.device)
     call("s2c_antialiased_cluster_bitset_grad", B, H, W, S, ptr(bitset), ptr(target_bitset), V, ptr(pos),
@@ -407,6 +407,20 @@ def dda_cluster_bitset(pos, edges, prim2cluster, bitset, edge_ids=None, ws=None)
     call("s2c_dda_cluster_bitset", P, ptr(edge_ids), H, W, B, V, ptr(pos), E, ptr(edges), ptr(prim2cluster), S,
          ptr(bitset), ptr(ws), ws.numel(), _stream(pos))
     return bitset
+
+
+def bitset_to_planes(bitset, planes=None) -> torch.Tensor:
+    """Cluster planes (B, 32 S, H, ceil(W / 32)) int32 of a bitset (B, H, W, S)."""
+    _arr(bitset, _i32, 4, name="bitset")
+    _cuda(bitset)
+    B, H, W, S = bitset.shape
+    shape = (B, 32 * S, H, (W + 31) // 32)
+    if planes is None:
+        planes = torch.empty(shape, dtype=torch.int32, device=bitset.device)
+    elif tuple(planes.shape) != shape or planes.dtype != _i32 or not planes.is_contiguous():
+        raise RuntimeError("bitset_to_planes: planes must be contiguous int32 " + str(shape))
+    call("s2c_bitset_to_planes", B, H, W, S, ptr(bitset), ptr(planes), _stream(bitset))
+    return planes
 
 
 def dda_cluster_bitset_stats(ws) -> tuple:

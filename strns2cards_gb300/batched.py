@@ -1,0 +1,226 @@
+"""Batched per-cluster card fitting: every cluster of a model is one view of one batch.
+
+The reference fits cards cluster by cluster (``3_fitting.py``: per cluster, a local
+orthographic frame, the strands' target bitset, the card raster, the antialiased-bitset
+gradient and a Laplacian-preconditioned step).  Here all clusters advance together: the
+clusters are the views ``b`` of single launches --
+
+* strands: vertices padded per cluster to ``(C, Vmax, 4)``; each cluster's own segments are
+  selected by ``edge_ids = b * E + e``, so padding is never read;
+* cards: ``(C, Vc, 4)`` with one shared grid topology;
+* one iteration = target coverage (fused DDA), card raster (fused), antialiased-bitset
+  gradient (fused), a gradient step on the card vertices, ``laplacian_steps`` Jacobi
+  Laplacian steps -- five sync-free launches groups, captured in one CUDA graph.
+
+``FitSchedule`` is the autotuner: it times the eager launch sequence, the single-stream
+graph and a two-stream graph (target coverage overlapped with the card raster) on the
+first iterations and keeps the fastest.  ``plain_iteration`` runs the same work as one
+call sequence per cluster, the per-call path this batching replaces.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _core, _lib
+from .dda import dda_cluster_bitset
+from .deform import CardLaplacian
+from .mesh import build_edges_from_triangles
+from .rasterize import rasterize_fused
+
+
+@dataclass
+class ClusterBatch:
+    """Host description of C clusters in their local frames (clip space, w = 1)."""
+    strand_pos: np.ndarray      # (C, Vmax, 4) float32, padded
+    strand_edges: np.ndarray    # (E, 2) int32, shared (strand polylines of the largest cluster)
+    edge_ids: np.ndarray        # (P,) int32, b * E + e of each cluster's own segments
+    card_pos: np.ndarray        # (C, Vc, 4) float32
+    card_tri: np.ndarray        # (Tc, 3) int32, shared
+    card_edges: np.ndarray      # (Ec, 2) int32, shared
+    card_e2t: np.ndarray        # (Ec, 2) int32
+    quad_edges: np.ndarray      # (Qe, 2) int32, local to one card
+    H: int
+    W: int
+
+
+def synthetic_clusters(num_clusters=256, verts=64, min_strands=20, max_strands=2000, quads_along=32,
+                       quads_across=4, H=512, W=128, seed=0) -> ClusterBatch:
+    """Clusters of log-uniform size in [min_strands, max_strands] (seed 0), each framed by
+    its own orthographic camera onto (W, H) = (128, 512), one 32 x 4-quad card each."""
+    from . import synthetic as syn
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(min_strands), np.log(max_strands), size=num_clusters)).astype(np.int64)
+    nmax = int(counts.max())
+    Vmax = nmax * verts
+    strand_pos = np.zeros((num_clusters, Vmax, 4), np.float32)
+    strand_pos[..., 3] = 1.0
+    E_one = verts - 1
+    edges = syn.strand_edges(nmax, verts)
+    edge_ids: List[np.ndarray] = []
+    faces, _, he, we = syn.grid_strip(quads_across + 1, quads_along + 1)
+    nv = (quads_across + 1) * (quads_along + 1)
+    card_pos = np.zeros((num_clusters, nv, 4), np.float32)
+    for c in range(num_clusters):
+        st = syn.make_strands(int(counts[c]), verts, seed=seed + 1 + c)
+        lo, hi = st.reshape(-1, 3).min(0), st.reshape(-1, 3).max(0)
+        ctr, half = (lo + hi) / 2, np.maximum((hi - lo) / 2, 1e-6) * 1.15
+        loc = (st.reshape(-1, 3) - ctr) / half                         # local frame in [-1/1.15, 1/1.15]
+        strand_pos[c, :loc.shape[0], :3] = loc.astype(np.float32)
+        strand_pos[c, :loc.shape[0], 2] *= 0.5
+        edge_ids.append((c * edges.shape[0] + np.arange(int(counts[c]) * E_one)).astype(np.int32))
+        cards = syn.make_cards(st, int(counts[c]), quads_along, quads_across)
+        cp = (cards.verts - ctr) / half
+        card_pos[c, :, :3] = cp.astype(np.float32)
+        card_pos[c, :, 2] *= 0.5
+        card_pos[c, :, 3] = 1.0
+    ce, ce2t = build_edges_from_triangles(faces.astype(np.int32))
+    return ClusterBatch(strand_pos, edges, np.concatenate(edge_ids), card_pos, faces.astype(np.int32), ce, ce2t,
+                        np.concatenate([he, we], 0).astype(np.int32), H, W)
+
+
+class BatchedClusterFit:
+    """Device state of a batched fit; ``step()`` runs one iteration for every cluster."""
+
+    def __init__(self, batch: ClusterBatch, device="cuda", lr: float = 1e-4, lam: float = 0.5,
+                 laplacian_steps: int = 10, kernel_radius: float = 7.0, rho: float = 1.0):
+        dev = torch.device(device)
+        self.batch = batch
+        self.C = batch.card_pos.shape[0]
+        self.H, self.W = batch.H, batch.W
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        self.spos, self.sedges, self.edge_ids = t(batch.strand_pos), t(batch.strand_edges), t(batch.edge_ids)
+        self.se2c = torch.zeros(batch.strand_edges.shape[0], dtype=torch.int32, device=dev)
+        self.cpos = t(batch.card_pos)
+        self.ctri, self.cedges, self.ce2t = t(batch.card_tri), t(batch.card_edges), t(batch.card_e2t)
+        self.ct2c = torch.zeros(batch.card_tri.shape[0], dtype=torch.int32, device=dev)
+        self.ce2c = torch.zeros(batch.card_edges.shape[0], dtype=torch.int32, device=dev)
+        C, H, W = self.C, self.H, self.W
+        L = _lib.lib()
+        self.target = torch.empty((C, H, W, 1), dtype=torch.int32, device=dev)
+        self.bits = torch.empty((C, H, W, 1), dtype=torch.int32, device=dev)
+        self.rast = None
+        self.d_pos = torch.zeros_like(self.cpos)
+        self.xyz = torch.empty((C * self.cpos.shape[1], 3), dtype=torch.float32, device=dev)
+        self.ws_dda = torch.empty(L.s2c_dda_cluster_bitset_workspace_size(self.edge_ids.shape[0], C, H, W, 1),
+                                  dtype=torch.uint8, device=dev)
+        self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(C, H, W, self.ctri.shape[0]),
+                                  dtype=torch.uint8, device=dev)
+        self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_workspace_size(C, self.cpos.shape[1], H, W, 1),
+                                 dtype=torch.uint8, device=dev)
+        self.lap = CardLaplacian(self.cpos.shape[1], batch.quad_edges, dev)
+        self.lr, self.lam, self.nlap = float(lr), float(lam), int(laplacian_steps)
+        self.kr, self.rho = float(kernel_radius), float(rho)
+        self.side = torch.cuda.Stream(device=dev)
+        self.graph = None
+        self.mode = "eager"
+
+    # -- the five parts of an iteration --
+    def _coverage(self):
+        dda_cluster_bitset((self.H, self.W), self.spos, self.sedges, self.se2c, 1, edge_ids=self.edge_ids,
+                           out=self.target, workspace=self.ws_dda)
+
+    def _raster(self):
+        rasterize_fused((self.H, self.W), self.cpos, self.ctri, self.ct2c, 1, want_rast=False, bitset=self.bits,
+                        workspace=self.ws_tri)
+
+    def _update(self):
+        self.d_pos.zero_()
+        _core.antialiased_cluster_bitset_grad(self.bits, self.target, self.cpos, self.ctri, self.cedges, self.ce2t,
+                                              self.ce2c, self.kr, self.rho, d_pos=self.d_pos, ws=self.ws_aa)
+        # gradient step on x, y, then Laplacian smoothing of every card
+        self.cpos[..., :2].sub_(self.d_pos[..., :2], alpha=self.lr)
+        self.xyz.copy_(self.cpos[..., :3].reshape(-1, 3))
+        self.lap(self.xyz, self.lam, self.nlap, out=self.xyz)
+        self.cpos[..., :3].copy_(self.xyz.view(self.C, -1, 3))
+
+    def eager_step(self, two_streams: bool = False):
+        if two_streams:
+            cur = torch.cuda.current_stream()
+            self.side.wait_stream(cur)
+            with torch.cuda.stream(self.side):
+                self._coverage()
+            self._raster()
+            cur.wait_stream(self.side)
+        else:
+            self._coverage()
+            self._raster()
+        self._update()
+
+    def capture(self, two_streams: bool = False):
+        """Capture one iteration in a CUDA graph (after a warm-up on the side stream)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.eager_step(two_streams)
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.eager_step(two_streams)
+        self.graph = g
+        return g
+
+    def step(self):
+        if self.mode.startswith("graph"):
+            self.graph.replay()
+        else:
+            self.eager_step(self.mode == "eager2")
+
+    def plain_iteration(self):
+        """The same iteration as C independent per-cluster call sequences."""
+        for c in range(self.C):
+            sl = slice(c, c + 1)
+            ids = self._plain_ids[c]
+            dda_cluster_bitset((self.H, self.W), self.spos[sl], self.sedges, self.se2c, 1, edge_ids=ids,
+                               out=self.target[sl])
+            rasterize_fused((self.H, self.W), self.cpos[sl], self.ctri, self.ct2c, 1, want_rast=False,
+                            bitset=self.bits[sl])
+            d = _core.antialiased_cluster_bitset_grad(self.bits[sl], self.target[sl], self.cpos[sl].contiguous(),
+                                                      self.ctri, self.cedges, self.ce2t, self.ce2c, self.kr, self.rho)
+            p = self.cpos[c]
+            p[:, :2].sub_(d[0, :, :2], alpha=self.lr)
+            xyz = p[:, :3].contiguous()
+            self.lap(xyz, self.lam, self.nlap, out=xyz)
+            p[:, :3].copy_(xyz)
+
+    def prepare_plain(self):
+        E = self.batch.strand_edges.shape[0]
+        ids = self.batch.edge_ids
+        b = ids // E
+        self._plain_ids = [torch.from_numpy((ids[b == c] - c * E).astype(np.int32)).to(self.spos.device)
+                           for c in range(self.C)]
+
+
+class FitSchedule:
+    """Autotuner over launch schedules of ``BatchedClusterFit.step``: eager, eager on two
+    streams, graph, graph on two streams.  Each is timed over ``trials`` iterations (CUDA
+    events) and the fastest is kept; the choice and timings are in ``self.results``."""
+
+    def __init__(self, fit: BatchedClusterFit, trials: int = 5):
+        self.fit = fit
+        self.results = {}
+        snap = fit.cpos.clone()
+        graphs = {}
+        for mode in ("eager", "eager2", "graph", "graph2"):
+            if mode.startswith("graph"):
+                graphs[mode] = fit.capture(two_streams=mode == "graph2")
+            fit.mode = mode
+            fit.graph = graphs.get(mode)
+            fit.step()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            for _ in range(trials):
+                fit.step()
+            b.record()
+            torch.cuda.synchronize()
+            self.results[mode] = a.elapsed_time(b) / trials
+        fit.cpos.copy_(snap)
+        best = min(self.results, key=self.results.get)
+        fit.mode = best
+        fit.graph = graphs.get(best)
+        self.best = best

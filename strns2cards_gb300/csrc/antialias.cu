@@ -88,8 +88,45 @@ struct AAArgs {
     const int32_t* __restrict__ e2c;
     float* __restrict__ d_pos;
     double* __restrict__ acc64;     // non-null: contributions summed in FP64 here instead
+    const uint32_t* __restrict__ pplanes;  // cluster planes of bitset / target (B, 32 S, H, WQ)
+    const uint32_t* __restrict__ tplanes;
+    int WQ;
     float kr, rho;
 };
+
+// Compensated FP32 sums (no FP64 arithmetic on the SMs: GB300's FP64 rate is a small
+// fraction of its FP32 rate).  kahan_add: running (sum, comp); two_sum_merge: error-free
+// merge of two compensated sums (Knuth's 2Sum on the leading parts).
+__device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
+    const float y = __fsub_rn(v, comp);
+    const float t = __fadd_rn(sum, y);
+    comp = __fsub_rn(__fsub_rn(t, sum), y);
+    sum = t;
+}
+
+__device__ __forceinline__ void two_sum_merge(float& hi, float& lo, float ohi, float olo) {
+    const float s = __fadd_rn(hi, ohi);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(ohi, bb));
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, olo), err);
+}
+
+// warp-wide compensated sum of the lanes' (sum, -comp) pairs, rounded to float
+__device__ __forceinline__ float warp_sum_comp(float sum, float comp) {
+    float hi = sum, lo = -comp;
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        const float ohi = __shfl_xor_sync(0xffffffffu, hi, off), olo = __shfl_xor_sync(0xffffffffu, lo, off);
+        two_sum_merge(hi, lo, ohi, olo);
+    }
+    return __fadd_rn(hi, lo);
+}
+
+__device__ __forceinline__ int plane_bit(const uint32_t* __restrict__ planes, const AAArgs& A, int b, int c, int y,
+                                         int x) {
+    return (__ldg(planes + (((int64_t)b * 32 * A.S + c) * A.H + y) * A.WQ + (x >> 5)) >> (x & 31)) & 1;
+}
 
 __device__ __forceinline__ int bit_of(const int32_t* __restrict__ bits, int64_t pix, int S, int c) {
     return (__ldg(bits + pix * S + (c >> 5)) >> (c & 31)) & 1;
@@ -101,12 +138,13 @@ __device__ __forceinline__ int bit_of(const int32_t* __restrict__ bits, int64_t 
 // false when the fragment contributes nothing; otherwise dc (on every lane) and the
 // quantities of the chain rule.
 struct AAFrag {
-    double dc;
+    float dc;
     float px, py, pw, t0, t1;
     float2 nrm;
     int2 ev;
 };
 
+template <bool kPlanes>
 __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w, float axis, float t1, int e,
                                             float2 nrm, int lane, AAFrag& o) {
     const float fH = (float)A.H, fW = (float)A.W;
@@ -138,8 +176,12 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
     const int c = __ldg(A.e2c + e);
     if (c < 0 || c >= 32 * A.S) return false;
     const int64_t img = (int64_t)b * A.H * A.W;
-    const int c01 = 1 - (dot > 0.f ? bit_of(A.bitset, img + (int64_t)nh * A.W + nw, A.S, c)
-                                   : bit_of(A.bitset, img + (int64_t)h * A.W + w, A.S, c));
+    int c01;
+    if (kPlanes)
+        c01 = 1 - (dot > 0.f ? plane_bit(A.pplanes, A, b, c, nh, nw) : plane_bit(A.pplanes, A, b, c, h, w));
+    else
+        c01 = 1 - (dot > 0.f ? bit_of(A.bitset, img + (int64_t)nh * A.W + nw, A.S, c)
+                             : bit_of(A.bitset, img + (int64_t)h * A.W + w, A.S, c));
     if (c01 == 0) return false;
     // Gaussian window (antialias.cu:121-176), taps spread over the warp
     const int R = f2i(floorf(A.kr));
@@ -154,7 +196,47 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
     // each lane sums its taps (at most ceil(taps / 32) of them) in FP32; the lanes' partial
     // sums are reduced in FP64.  Tap j = lane + 32 i sits at (row, col) = divmod(j, ww),
     // stepped incrementally.
-    float part = 0.f;
+    if (kPlanes) {
+        // lanes take window rows; a row is read as the 1-2 plane words covering [w0, w1) of
+        // both images, and only the pixels where they differ are visited, in x order
+        float sum = 0.f, comp = 0.f;
+        const int rows = taps > 0 ? h1 - h0 : 0;
+        const int64_t pbase = ((int64_t)b * 32 * A.S + c) * A.H;
+        for (int r = lane; r < rows; r += 32) {
+            const int th = h0 + r;
+            const uint32_t* prow = A.pplanes + (pbase + th) * A.WQ;
+            const uint32_t* trow = A.tplanes + (pbase + th) * A.WQ;
+            const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), fy);
+            for (int q = w0 >> 5; q <= (w1 - 1) >> 5; ++q) {
+                const int lo = max(w0 - 32 * q, 0), hi = min(w1 - 32 * q, 32);
+                const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+                const uint32_t pv = __ldg(prow + q), tv = __ldg(trow + q);
+                const uint32_t pos = pv & ~tv & m, neg = ~pv & tv & m;
+                uint32_t any = pos | neg;
+                while (any) {
+                    const int bit = __ffs(any) - 1;
+                    any &= any - 1;
+                    const int tw = 32 * q + bit;
+                    const float dx = __fsub_rn(__fadd_rn((float)tw, 0.5f), fx);
+                    const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+                    if (!(n2 < kr2)) continue;
+                    const float wgt = __fmul_rn(cc, expf(-alpha * n2));
+                    kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, A.rho) : -wgt);
+                }
+            }
+        }
+        o.dc = __fmul_rn((float)c01, warp_sum_comp(sum, comp));
+        if (o.dc == 0.f) return false;
+        o.px = px;
+        o.py = py;
+        o.pw = pw;
+        o.t0 = t0;
+        o.t1 = t1;
+        o.nrm = nrm;
+        o.ev = ev;
+        return true;
+    }
+    float sum = 0.f, comp = 0.f;
     if (taps > 0) {
         const int s_row = 32 / ww, s_col = 32 - s_row * ww;
         int row = lane / ww, col = lane - (lane / ww) * ww;
@@ -175,15 +257,11 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
             const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
             if (!(n2 < kr2)) continue;
             const float wgt = __fmul_rn(cc, expf(-alpha * n2));
-            const float sgn = c0 ? (c1 ? 0.f : A.rho) : -1.f;   // (c0 - c1) * (c1 == 0 ? rho : 1)
-            part = __fmaf_rn(wgt, sgn, part);
+            kahan_add(sum, comp, c0 ? __fmul_rn(wgt, A.rho) : -wgt);   // (c0 - c1) * (c1 == 0 ? rho : 1)
         }
     }
-    double acc = (double)part;
-#pragma unroll
-    for (int off = 16; off; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    o.dc = (double)c01 * acc;
-    if (o.dc == 0.0) return false;
+    o.dc = __fmul_rn((float)c01, warp_sum_comp(sum, comp));
+    if (o.dc == 0.f) return false;
     o.px = px;
     o.py = py;
     o.pw = pw;
@@ -194,15 +272,15 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
     return true;
 }
 
-// FP64 chain rule of one fragment: (d/dx, d/dy, d/dw) of the edge point, false if not finite
-__device__ __forceinline__ bool aa_chain64(const AAArgs& A, const AAFrag& f, double& qx, double& qy, double& qw) {
-    const double dxd = f.dc * 0.5 * (double)A.W * (double)f.nrm.x;
-    const double dyd = f.dc * -0.5 * (double)A.H * (double)f.nrm.y;
-    const double pwd = (double)f.pw;
-    qx = dxd / pwd;
-    qy = dyd / pwd;
-    qw = (dxd * (double)f.px + dyd * (double)f.py) / (pwd * pwd);
-    return isfinite(qx) && isfinite(qy) && isfinite(qw);
+// Chain rule of one fragment in FP32 (antialias.cu:281-316): (d/dx, d/dy, d/dw) of the
+// edge point; false if not finite
+__device__ __forceinline__ bool aa_chain(const AAArgs& A, const AAFrag& f, float& dpx, float& dpy, float& dpw) {
+    const float dx = __fmul_rn(__fmul_rn(__fmul_rn(f.dc, 0.5f), (float)A.W), f.nrm.x);
+    const float dy = __fmul_rn(__fmul_rn(__fmul_rn(f.dc, -0.5f), (float)A.H), f.nrm.y);
+    dpx = __fdiv_rn(dx, f.pw);
+    dpy = __fdiv_rn(dy, f.pw);
+    dpw = __fdiv_rn(__fmaf_rn(dx, f.px, __fmul_rn(dy, f.py)), __fmul_rn(f.pw, f.pw));
+    return isfinite(dpx) && isfinite(dpy) && isfinite(dpw);
 }
 
 // antialias.cu:121-279, one warp per fragment of a fragment list
@@ -215,33 +293,26 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
         const int fb = A.frag_pix[3 * i], fe = f2i(fa.w) - 1;
         if (fe < 0 || fe >= A.E || fb < 0 || fb >= A.B) continue;
         AAFrag f;
-        if (!aa_fragment(A, fb, A.frag_pix[3 * i + 1], A.frag_pix[3 * i + 2], fa.x, fa.y, fe,
+        if (!aa_fragment<false>(A, fb, A.frag_pix[3 * i + 1], A.frag_pix[3 * i + 2], fa.x, fa.y, fe,
                          __ldg(A.normals + (int64_t)fb * A.E + fe), lane, f))
             continue;
         if (lane != 0) continue;
+        float dpx, dpy, dpw;
+        if (!aa_chain(A, f, dpx, dpy, dpw)) continue;
+        const int b = A.frag_pix[3 * i];
         if (A.acc64) {
-            // chain rule and accumulation in FP64 (no cancellation loss across fragments)
-            double qx, qy, qw;
-            if (!aa_chain64(A, f, qx, qy, qw)) continue;
-            const int b = A.frag_pix[3 * i];
+            // contributions summed in FP64 at the L2 (no cancellation loss across fragments)
             double* a0 = A.acc64 + ((int64_t)b * A.V + f.ev.x) * 3;
             double* a1 = A.acc64 + ((int64_t)b * A.V + f.ev.y) * 3;
-            atomicAdd(a0 + 0, qx * (double)f.t0);
-            atomicAdd(a0 + 1, qy * (double)f.t0);
-            atomicAdd(a0 + 2, qw * (double)f.t0);
-            atomicAdd(a1 + 0, qx * (double)f.t1);
-            atomicAdd(a1 + 1, qy * (double)f.t1);
-            atomicAdd(a1 + 2, qw * (double)f.t1);
+            atomicAdd(a0 + 0, (double)__fmul_rn(dpx, f.t0));
+            atomicAdd(a0 + 1, (double)__fmul_rn(dpy, f.t0));
+            atomicAdd(a0 + 2, (double)__fmul_rn(dpw, f.t0));
+            atomicAdd(a1 + 0, (double)__fmul_rn(dpx, f.t1));
+            atomicAdd(a1 + 1, (double)__fmul_rn(dpy, f.t1));
+            atomicAdd(a1 + 2, (double)__fmul_rn(dpw, f.t1));
             continue;
         }
-        // FP32 chain rule and float atomics, as the reference
-        const float dcf = (float)f.dc;
-        const float dx = __fmul_rn(__fmul_rn(__fmul_rn(dcf, 0.5f), (float)A.W), f.nrm.x);
-        const float dy = __fmul_rn(__fmul_rn(__fmul_rn(dcf, -0.5f), (float)A.H), f.nrm.y);
-        const float dpx = __fdiv_rn(dx, f.pw), dpy = __fdiv_rn(dy, f.pw);
-        const float dpw = __fdiv_rn(__fmaf_rn(dx, f.px, __fmul_rn(dy, f.py)), __fmul_rn(f.pw, f.pw));
-        if (!isfinite(dpx) || !isfinite(dpy) || !isfinite(dpw)) continue;
-        const int b = A.frag_pix[3 * i];
+        // float atomics, as the reference
         float* g0 = A.d_pos + ((int64_t)b * A.V + f.ev.x) * 4;
         float* g1 = A.d_pos + ((int64_t)b * A.V + f.ev.y) * 4;
         atomicAdd(g0 + 0, __fmul_rn(dpx, f.t0));
@@ -255,8 +326,9 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
 
 // Fused edge gradient: one warp per (view, edge).  The mark test, the edge's DDA walk
 // (the fragments dda_compute_fragments + filter_valid_fragments would list) and each
-// fragment's window run in registers; the edge's contributions are summed in FP64 and
-// added to the FP64 accumulator once per edge.  No fragment list, no host round trip.
+// fragment's window (read from cluster planes) run in registers; the edge's contributions
+// are summed with compensation and added to the FP64 accumulator once per edge.  No
+// fragment list, no host round trip.
 __global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -271,7 +343,8 @@ __global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
         const float4 p0 = __ldg(M.pos4 + (int64_t)b * M.V + ev.x), p1 = __ldg(M.pos4 + (int64_t)b * M.V + ev.y);
         const Span sp = dda_span(p0, p1, A.H, A.W);
         const int ee = prim_roundtrip(e);
-        double s0x = 0.0, s0y = 0.0, s0w = 0.0, s1x = 0.0, s1y = 0.0, s1w = 0.0;
+        // the edge's six sums, compensated FP32 on lane 0 (sum, comp)
+        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, cmp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         bool any = false;
         for (int k = 0; k < sp.count; ++k) {
             float x, y;
@@ -281,28 +354,27 @@ __global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
             const float t1 = dda_t1(p0, p1, x, y, sp.axis, A.H, A.W);
             if (!z_ok(dda_z(p0, p1, t1))) continue;
             AAFrag f;
-            if (!aa_fragment(A, b, h, w, sp.axis, t1, ee, nrm, lane, f)) continue;
+            if (!aa_fragment<true>(A, b, h, w, sp.axis, t1, ee, nrm, lane, f)) continue;
             if (lane != 0) continue;
-            double qx, qy, qw;
-            if (!aa_chain64(A, f, qx, qy, qw)) continue;
-            s0x += qx * (double)f.t0;
-            s0y += qy * (double)f.t0;
-            s0w += qw * (double)f.t0;
-            s1x += qx * (double)f.t1;
-            s1y += qy * (double)f.t1;
-            s1w += qw * (double)f.t1;
+            float dpx, dpy, dpw;
+            if (!aa_chain(A, f, dpx, dpy, dpw)) continue;
+            kahan_add(acc[0], cmp[0], __fmul_rn(dpx, f.t0));
+            kahan_add(acc[1], cmp[1], __fmul_rn(dpy, f.t0));
+            kahan_add(acc[2], cmp[2], __fmul_rn(dpw, f.t0));
+            kahan_add(acc[3], cmp[3], __fmul_rn(dpx, f.t1));
+            kahan_add(acc[4], cmp[4], __fmul_rn(dpy, f.t1));
+            kahan_add(acc[5], cmp[5], __fmul_rn(dpw, f.t1));
             any = true;
         }
         if (lane == 0 && any) {
             const int2 evv = __ldg(A.edges + ee);
             double* a0 = A.acc64 + ((int64_t)b * A.V + evv.x) * 3;
             double* a1 = A.acc64 + ((int64_t)b * A.V + evv.y) * 3;
-            atomicAdd(a0 + 0, s0x);
-            atomicAdd(a0 + 1, s0y);
-            atomicAdd(a0 + 2, s0w);
-            atomicAdd(a1 + 0, s1x);
-            atomicAdd(a1 + 1, s1y);
-            atomicAdd(a1 + 2, s1w);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                atomicAdd(a0 + q, (double)acc[q] - (double)cmp[q]);
+                atomicAdd(a1 + q, (double)acc[3 + q] - (double)cmp[3 + q]);
+            }
         }
     }
 }
@@ -425,23 +497,21 @@ extern "C" s2c_status s2c_backward_antialiased_cluster_bitset_f64(
                        d_pos, kernel_radius, rho, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
-extern "C" size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V) {
-    return (size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3 * sizeof(double);
+extern "C" size_t s2c_antialiased_cluster_bitset_grad_planes_workspace_size(int B, int V) {
+    return (size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3 * sizeof(double) + 256;
 }
 
-extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, int S, const int32_t* bitset,
-                                                          const int32_t* target, int V, const float* pos, int T,
-                                                          const int32_t* tri, int E, const int32_t* edges,
-                                                          const int32_t* edge2tri, const int32_t* edge2cluster,
-                                                          float* d_pos, float kernel_radius, float rho,
-                                                          void* workspace, size_t workspace_bytes,
-                                                          s2c_stream stream) {
+extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
+    int B, int H, int W, int S, const uint32_t* bitset_planes, const uint32_t* target_planes, int V, const float* pos,
+    int T, const int32_t* tri, int E, const int32_t* edges, const int32_t* edge2tri, const int32_t* edge2cluster,
+    float* d_pos, float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream) {
     S2C_REQUIRE(B > 0 && H > 0 && W > 0 && S > 0 && V >= 0 && T >= 0 && E >= 0,
                 "antialiased_cluster_bitset_grad: bad sizes");
     const int64_t BE = (int64_t)B * E, BV = (int64_t)B * V;
     S2C_REQUIRE(BE < (1LL << 31), "antialiased_cluster_bitset_grad: B*E too large");
     if (BE == 0 || BV == 0) return S2C_OK;
-    S2C_REQUIRE(bitset && target && pos && edges && edge2tri && edge2cluster && d_pos && (T == 0 || tri) && workspace,
+    S2C_REQUIRE(bitset_planes && target_planes && pos && edges && edge2tri && edge2cluster && d_pos &&
+                    (T == 0 || tri) && workspace,
                 "antialiased_cluster_bitset_grad: null pointer");
     S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && ((uintptr_t)edges & 7) == 0 && ((uintptr_t)edge2tri & 7) == 0 &&
                     ((uintptr_t)workspace & 7) == 0,
@@ -468,16 +538,16 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, i
     A.H = H;
     A.W = W;
     A.S = S;
-    A.bitset = bitset;
-    A.target = target;
     A.pos4 = (const float4*)pos;
     A.V = V;
     A.E = E;
     A.edges = (const int2*)edges;
-    A.normals = nullptr;
     A.e2c = edge2cluster;
     A.d_pos = d_pos;
     A.acc64 = (double*)workspace;
+    A.pplanes = bitset_planes;
+    A.tplanes = target_planes;
+    A.WQ = (W + 31) / 32;
     A.kr = kernel_radius;
     A.rho = rho;
     const int64_t warps = std::min<int64_t>(BE, (int64_t)num_sms() * 64);
@@ -486,4 +556,33 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, i
     aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, (const double*)workspace, d_pos);
     S2C_CHECK_LAUNCH("aa_finalize_kernel");
     return S2C_OK;
+}
+
+extern "C" size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S) {
+    const size_t planes = s2c_bitset_planes_size(B, H, W, S);
+    return align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V), 256) + 2 * align_up(planes, 256);
+}
+
+extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, int S, const int32_t* bitset,
+                                                          const int32_t* target, int V, const float* pos, int T,
+                                                          const int32_t* tri, int E, const int32_t* edges,
+                                                          const int32_t* edge2tri, const int32_t* edge2cluster,
+                                                          float* d_pos, float kernel_radius, float rho,
+                                                          void* workspace, size_t workspace_bytes,
+                                                          s2c_stream stream) {
+    S2C_REQUIRE(B > 0 && H > 0 && W > 0 && S > 0, "antialiased_cluster_bitset_grad: bad sizes");
+    S2C_REQUIRE(bitset && target && workspace, "antialiased_cluster_bitset_grad: null pointer");
+    const size_t need = s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S);
+    S2C_REQUIRE(workspace_bytes >= need, "antialiased_cluster_bitset_grad: workspace of %zu bytes, need %zu",
+                workspace_bytes, need);
+    const size_t acc = align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V), 256);
+    const size_t planes = align_up(s2c_bitset_planes_size(B, H, W, S), 256);
+    uint32_t* pp = (uint32_t*)((char*)workspace + acc);
+    uint32_t* tp = (uint32_t*)((char*)workspace + acc + planes);
+    s2c_status s = s2c_bitset_to_planes(B, H, W, S, bitset, pp, stream);
+    if (s == S2C_OK) s = s2c_bitset_to_planes(B, H, W, S, target, tp, stream);
+    if (s != S2C_OK) return s;
+    return s2c_antialiased_cluster_bitset_grad_planes(B, H, W, S, pp, tp, V, pos, T, tri, E, edges, edge2tri,
+                                                      edge2cluster, d_pos, kernel_radius, rho, workspace, acc,
+                                                      stream);
 }

@@ -172,6 +172,56 @@ __global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, i
     }
 }
 
+// ---- cluster planes ----------------------------------------------------------------------
+// planes (B, 32 S, H, WQ) uint32, WQ = ceil(W / 32): bit (x & 31) of word x >> 5 of row y
+// of plane c is bit c of pixel (y, x).  A CTA takes one image row, 512 pixels and 8 slots:
+// the tile is read with whole 32-byte runs per pixel, each warp turns (32 pixels x 32
+// clusters) blocks around with a 5-stage shuffle bit transpose, and the plane rows are
+// written contiguously.
+constexpr int kPlaneX = 512, kPlaneS = 8;
+
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+    // recursive block swap: after the stage for j, blocks j x j apart are exchanged
+#pragma unroll
+    for (int j = 16; j; j >>= 1) {
+        const uint32_t m = j == 16 ? 0xFFFF0000u : j == 8 ? 0xFF00FF00u : j == 4 ? 0xF0F0F0F0u
+                         : j == 2 ? 0xCCCCCCCCu : 0xAAAAAAAAu;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        x = (lane & j) ? ((x & m) | ((y >> j) & ~m)) : ((x & ~m) | ((y << j) & m));
+    }
+    return x;
+}
+
+__global__ void __launch_bounds__(256) bitset_to_planes_kernel(int B, int H, int W, int S,
+                                                               const int32_t* __restrict__ bitset,
+                                                               uint32_t* __restrict__ planes) {
+    __shared__ uint32_t tin[kPlaneX][kPlaneS + 1];
+    __shared__ uint32_t tout[kPlaneS][32][kPlaneX / 32 + 1];
+    const int WQ = (W + 31) >> 5;
+    const int nxt = (W + kPlaneX - 1) / kPlaneX;
+    const int xt = blockIdx.x % nxt, st = blockIdx.x / nxt;
+    const int x0 = xt * kPlaneX, s0 = st * kPlaneS;
+    const int y = blockIdx.y, b = blockIdx.z;
+    const int64_t row = ((int64_t)b * H + y) * W;
+    for (int i = threadIdx.x; i < kPlaneX * kPlaneS; i += blockDim.x) {
+        const int p = i / kPlaneS, sl = i - p * kPlaneS;
+        const int x = x0 + p, s = s0 + sl;
+        tin[p][sl] = (x < W && s < S) ? (uint32_t)__ldg(bitset + (row + x) * S + s) : 0u;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;   // warp = slot within the tile
+#pragma unroll 4
+    for (int g = 0; g < kPlaneX / 32; ++g) tout[warp][lane][g] = transpose32(tin[32 * g + lane][warp], lane);
+    __syncthreads();
+    const int Kp = 32 * S;
+    for (int i = threadIdx.x; i < kPlaneS * 32 * (kPlaneX / 32); i += blockDim.x) {
+        const int g = i % (kPlaneX / 32), bit = (i / (kPlaneX / 32)) % 32, sl = i / (32 * (kPlaneX / 32));
+        const int s = s0 + sl, q = (x0 >> 5) + g;
+        if (s >= S || q >= WQ) continue;
+        planes[(((int64_t)b * Kp + 32 * s + bit) * H + y) * WQ + q] = tout[sl][bit][g];
+    }
+}
+
 }  // namespace s2c
 
 using namespace s2c;
@@ -231,5 +281,23 @@ extern "C" s2c_status s2c_accumulate_bitset_rgb(int64_t npix, int S, const int32
     S2C_REQUIRE(bitset && accum && (K == 0 || rgb), "accumulate_bitset_rgb: null pointer");
     accumulate_rgb_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(npix, S, bitset, K, rgb, accum);
     S2C_CHECK_LAUNCH("accumulate_rgb_kernel");
+    return S2C_OK;
+}
+
+extern "C" size_t s2c_bitset_planes_size(int B, int H, int W, int S) {
+    if (B <= 0 || H <= 0 || W <= 0 || S <= 0) return 0;
+    return (size_t)B * 32 * S * H * ((W + 31) / 32) * sizeof(uint32_t);
+}
+
+extern "C" s2c_status s2c_bitset_to_planes(int B, int H, int W, int S, const int32_t* bitset, uint32_t* planes,
+                                           s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && S > 0 && H <= 65535 && B <= 65535, "bitset_to_planes: bad sizes");
+    if (B == 0 || H == 0 || W == 0) return S2C_OK;
+    S2C_REQUIRE(bitset && planes, "bitset_to_planes: null pointer");
+    const int nxt = (W + kPlaneX - 1) / kPlaneX, nst = (S + kPlaneS - 1) / kPlaneS;
+    S2C_REQUIRE((int64_t)nxt * nst < (1LL << 31), "bitset_to_planes: too many tiles");
+    dim3 grid((unsigned)(nxt * nst), (unsigned)H, (unsigned)B);
+    bitset_to_planes_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(B, H, W, S, bitset, planes);
+    S2C_CHECK_LAUNCH("bitset_to_planes_kernel");
     return S2C_OK;
 }
