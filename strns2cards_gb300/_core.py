@@ -332,7 +332,7 @@ def antialiased_cluster_bitset_grad(bitset, target_bitset, pos, tri, edges, edge
     V = pos.shape[1]
     if d_pos is None:
         d_pos = torch.zeros_like(pos)
-    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S)
+    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S, edges.shape[0])
     if ws is None or ws.numel() < need:
         ws = workspace(need, pos.device)
     call("s2c_antialiased_cluster_bitset_grad", B, H, W, S, ptr(bitset), ptr(target_bitset), V, ptr(pos),

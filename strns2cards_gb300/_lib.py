@@ -57,8 +57,8 @@ SIGNATURES = {
     "s2c_backward_antialiased_cluster_bitset_workspace_size": ([c_i, c_i], c_sz),
     "s2c_backward_antialiased_cluster_bitset_f64": ([c_i64, vp, vp, c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp,
                                                      vp, vp, c_f, c_f, vp, c_sz, vp], c_i),
-    "s2c_antialiased_cluster_bitset_grad_workspace_size": ([c_i, c_i, c_i, c_i, c_i], c_sz),
-    "s2c_antialiased_cluster_bitset_grad_planes_workspace_size": ([c_i, c_i], c_sz),
+    "s2c_antialiased_cluster_bitset_grad_workspace_size": ([c_i, c_i, c_i, c_i, c_i, c_i], c_sz),
+    "s2c_antialiased_cluster_bitset_grad_planes_workspace_size": ([c_i, c_i, c_i], c_sz),
     "s2c_antialiased_cluster_bitset_grad_planes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, c_i, vp, vp, vp,
                                                     vp, c_f, c_f, vp, c_sz, vp], c_i),
     "s2c_bitset_planes_size": ([c_i, c_i, c_i, c_i], c_sz),

@@ -19,9 +19,8 @@ call sequence per cluster, the per-call path this batching replaces.
 """
 from __future__ import annotations
 
-import time
 from dataclasses import dataclass
-from typing import List, Optional
+from typing import List
 
 import numpy as np
 import torch
@@ -110,8 +109,9 @@ class BatchedClusterFit:
                                   dtype=torch.uint8, device=dev)
         self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(C, H, W, self.ctri.shape[0]),
                                   dtype=torch.uint8, device=dev)
-        self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_workspace_size(C, self.cpos.shape[1], H, W, 1),
-                                 dtype=torch.uint8, device=dev)
+        aa_need = L.s2c_antialiased_cluster_bitset_grad_workspace_size(C, self.cpos.shape[1], H, W, 1,
+                                                                         self.cedges.shape[0])
+        self.ws_aa = torch.empty(aa_need, dtype=torch.uint8, device=dev)
         self.lap = CardLaplacian(self.cpos.shape[1], batch.quad_edges, dev)
         self.lr, self.lam, self.nlap = float(lr), float(lam), int(laplacian_steps)
         self.kr, self.rho = float(kernel_radius), float(rho)

@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "scan.cuh"
 
 namespace s2c {
 
@@ -324,17 +325,49 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
     }
 }
 
-// Fused edge gradient: one warp per (view, edge).  The mark test, the edge's DDA walk
-// (the fragments dda_compute_fragments + filter_valid_fragments would list) and each
-// fragment's window (read from cluster planes) run in registers; the edge's contributions
-// are summed with compensation and added to the FP64 accumulator once per edge.  No
-// fragment list, no host round trip.
-__global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
+// Fused edge gradient.  Pass 1 (thread per (view, edge)): the mark test and the DDA span
+// count, as a number of chunks of kAAChunk fragments; a device scan; pass 2 (warp per
+// chunk): the chunk's fragments (those dda_compute_fragments + filter_valid_fragments
+// would list) through their windows read from cluster planes, the contributions summed
+// with compensation and added to the FP64 accumulator once per chunk.  Long edges spread
+// over many warps; no fragment list, no host round trip.
+constexpr int kAAChunk = 8;
+
+__global__ void __launch_bounds__(256) aa_chunk_count_kernel(AAArgs A, Mesh M, int32_t* __restrict__ chunks) {
+    const int64_t BE = (int64_t)A.B * M.E;
+    for (int64_t pe = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pe < BE; pe += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)M.divE.div((uint32_t)pe);
+        const int e = (int)pe - b * M.E;
+        float2 nrm;
+        int n = 0;
+        if (mark_edge(A.H, A.W, M, b, e, nrm) == 2) {
+            const int2 ev = __ldg(M.edges + e);
+            const Span sp = dda_span(__ldg(M.pos4 + (int64_t)b * M.V + ev.x), __ldg(M.pos4 + (int64_t)b * M.V + ev.y),
+                                     A.H, A.W);
+            n = (sp.count + kAAChunk - 1) / kAAChunk;
+        }
+        chunks[pe] = n;
+    }
+}
+
+__global__ void __launch_bounds__(256) aa_chunk_kernel(AAArgs A, Mesh M, const int32_t* __restrict__ prefix,
+                                                       const int64_t* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t BE = (int64_t)A.B * M.E;
-    for (int64_t pe = warp0; pe < BE; pe += nwarps) {
+    const int64_t nch = *total;
+    for (int64_t ch = warp0; ch < nch; ch += nwarps) {
+        // owner edge: first pe whose inclusive prefix exceeds ch
+        int64_t lo = 0, hi = BE;
+        while (lo < hi) {
+            const int64_t mid = (lo + hi) >> 1;
+            if ((int64_t)__ldg(prefix + mid) <= ch) lo = mid + 1;
+            else hi = mid;
+        }
+        if (lo >= BE) continue;
+        const int64_t pe = lo;
+        const int64_t first = pe > 0 ? (int64_t)__ldg(prefix + pe - 1) : 0;
         const int b = (int)M.divE.div((uint32_t)pe);
         const int e = (int)pe - b * M.E;
         float2 nrm;
@@ -343,10 +376,10 @@ __global__ void __launch_bounds__(256) aa_fused_kernel(AAArgs A, Mesh M) {
         const float4 p0 = __ldg(M.pos4 + (int64_t)b * M.V + ev.x), p1 = __ldg(M.pos4 + (int64_t)b * M.V + ev.y);
         const Span sp = dda_span(p0, p1, A.H, A.W);
         const int ee = prim_roundtrip(e);
-        // the edge's six sums, compensated FP32 on lane 0 (sum, comp)
+        const int k0 = (int)(ch - first) * kAAChunk, k1 = min(k0 + kAAChunk, sp.count);
         float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, cmp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         bool any = false;
-        for (int k = 0; k < sp.count; ++k) {
+        for (int k = k0; k < k1; ++k) {
             float x, y;
             dda_sample(sp, k, x, y);
             const int h = f2i(floorf(y)), w = f2i(floorf(x));
@@ -497,8 +530,31 @@ extern "C" s2c_status s2c_backward_antialiased_cluster_bitset_f64(
                        d_pos, kernel_radius, rho, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
-extern "C" size_t s2c_antialiased_cluster_bitset_grad_planes_workspace_size(int B, int V) {
-    return (size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3 * sizeof(double) + 256;
+namespace {
+struct AAWs {
+    double* acc;
+    int32_t* chunks;
+    int32_t* prefix;
+    int64_t* total;
+    void* scan;
+};
+
+size_t aa_carve(int B, int V, int E, void* base, size_t cap, AAWs* w) {
+    Carver cv(base, cap);
+    AAWs a;
+    const int64_t BE = std::max<int64_t>((int64_t)(B > 0 ? B : 0) * (E > 0 ? E : 0), 1);
+    a.acc = cv.take<double>((size_t)(B > 0 ? B : 0) * (size_t)(V > 0 ? V : 0) * 3);
+    a.chunks = cv.take<int32_t>(BE);
+    a.prefix = cv.take<int32_t>(BE);
+    a.total = cv.take<int64_t>(1);
+    a.scan = cv.take<char>(scan_workspace_bytes(BE));
+    if (w) *w = a;
+    return cv.off;
+}
+}  // namespace
+
+extern "C" size_t s2c_antialiased_cluster_bitset_grad_planes_workspace_size(int B, int V, int E) {
+    return aa_carve(B, V, E, nullptr, (size_t)-1, nullptr) + 256;
 }
 
 extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
@@ -517,11 +573,12 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
                     ((uintptr_t)workspace & 7) == 0,
                 "antialiased_cluster_bitset_grad: misaligned");
     S2C_REQUIRE(kernel_radius >= 0.f && kernel_radius < 1024.f, "antialiased_cluster_bitset_grad: bad kernel_radius");
-    S2C_REQUIRE(workspace_bytes >= (size_t)BV * 3 * sizeof(double),
-                "antialiased_cluster_bitset_grad: workspace of %zu bytes, need %lld", workspace_bytes,
-                (long long)(BV * 3 * sizeof(double)));
+    AAWs ws;
+    const size_t need = aa_carve(B, V, E, workspace, workspace_bytes, &ws);
+    S2C_REQUIRE(need <= workspace_bytes, "antialiased_cluster_bitset_grad: workspace of %zu bytes, need %zu",
+                workspace_bytes, need);
     cudaStream_t st = (cudaStream_t)stream;
-    cudaError_t e = cudaMemsetAsync(workspace, 0, (size_t)BV * 3 * sizeof(double), st);
+    cudaError_t e = cudaMemsetAsync(ws.acc, 0, (size_t)BV * 3 * sizeof(double), st);
     if (e != cudaSuccess) return cuda_status(e, "antialiased_cluster_bitset_grad: memset");
     Mesh M;
     M.pos4 = (const float4*)pos;
@@ -544,23 +601,27 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
     A.edges = (const int2*)edges;
     A.e2c = edge2cluster;
     A.d_pos = d_pos;
-    A.acc64 = (double*)workspace;
+    A.acc64 = ws.acc;
     A.pplanes = bitset_planes;
     A.tplanes = target_planes;
     A.WQ = (W + 31) / 32;
     A.kr = kernel_radius;
     A.rho = rho;
-    const int64_t warps = std::min<int64_t>(BE, (int64_t)num_sms() * 64);
-    aa_fused_kernel<<<grid_for(warps * 32, 256), 256, 0, st>>>(A, M);
-    S2C_CHECK_LAUNCH("aa_fused_kernel");
-    aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, (const double*)workspace, d_pos);
+    aa_chunk_count_kernel<<<grid_for(BE, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(A, M, ws.chunks);
+    S2C_CHECK_LAUNCH("aa_chunk_count_kernel");
+    s2c_status ss = inclusive_scan_i32(ws.chunks, BE, ws.prefix, ws.scan, ws.total, st);
+    if (ss != S2C_OK) return ss;
+    aa_chunk_kernel<<<num_sms() * 8, 256, 0, st>>>(A, M, ws.prefix, ws.total);
+    S2C_CHECK_LAUNCH("aa_chunk_kernel");
+    aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, ws.acc, d_pos);
     S2C_CHECK_LAUNCH("aa_finalize_kernel");
     return S2C_OK;
 }
 
-extern "C" size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S) {
+extern "C" size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S, int E) {
     const size_t planes = s2c_bitset_planes_size(B, H, W, S);
-    return align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V), 256) + 2 * align_up(planes, 256);
+    return align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V, E), 256) +
+           2 * align_up(planes, 256);
 }
 
 extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, int S, const int32_t* bitset,
@@ -572,10 +633,10 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad(int B, int H, int W, i
                                                           s2c_stream stream) {
     S2C_REQUIRE(B > 0 && H > 0 && W > 0 && S > 0, "antialiased_cluster_bitset_grad: bad sizes");
     S2C_REQUIRE(bitset && target && workspace, "antialiased_cluster_bitset_grad: null pointer");
-    const size_t need = s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S);
+    const size_t need = s2c_antialiased_cluster_bitset_grad_workspace_size(B, V, H, W, S, E);
     S2C_REQUIRE(workspace_bytes >= need, "antialiased_cluster_bitset_grad: workspace of %zu bytes, need %zu",
                 workspace_bytes, need);
-    const size_t acc = align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V), 256);
+    const size_t acc = align_up(s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V, E), 256);
     const size_t planes = align_up(s2c_bitset_planes_size(B, H, W, S), 256);
     uint32_t* pp = (uint32_t*)((char*)workspace + acc);
     uint32_t* tp = (uint32_t*)((char*)workspace + acc + planes);
