@@ -203,10 +203,24 @@ __global__ void __launch_bounds__(256) bitset_to_planes_kernel(int B, int H, int
     const int x0 = xt * kPlaneX, s0 = st * kPlaneS;
     const int y = blockIdx.y, b = blockIdx.z;
     const int64_t row = ((int64_t)b * H + y) * W;
-    for (int i = threadIdx.x; i < kPlaneX * kPlaneS; i += blockDim.x) {
-        const int p = i / kPlaneS, sl = i - p * kPlaneS;
-        const int x = x0 + p, s = s0 + sl;
-        tin[p][sl] = (x < W && s < S) ? (uint32_t)__ldg(bitset + (row + x) * S + s) : 0u;
+    if ((S & 3) == 0 && (((uintptr_t)bitset) & 15) == 0) {
+        // 16-byte loads: pixel p's 8 slots are two int4 (S a multiple of 4)
+        for (int i = threadIdx.x; i < kPlaneX * (kPlaneS / 4); i += blockDim.x) {
+            const int p = i >> 1, h = i & 1;
+            const int x = x0 + p, s = s0 + 4 * h;
+            int4 v = make_int4(0, 0, 0, 0);
+            if (x < W && s < S) v = __ldg((const int4*)(bitset + (row + x) * S + s));
+            tin[p][4 * h] = (uint32_t)v.x;
+            tin[p][4 * h + 1] = (uint32_t)v.y;
+            tin[p][4 * h + 2] = (uint32_t)v.z;
+            tin[p][4 * h + 3] = (uint32_t)v.w;
+        }
+    } else {
+        for (int i = threadIdx.x; i < kPlaneX * kPlaneS; i += blockDim.x) {
+            const int p = i / kPlaneS, sl = i - p * kPlaneS;
+            const int x = x0 + p, s = s0 + sl;
+            tin[p][sl] = (x < W && s < S) ? (uint32_t)__ldg(bitset + (row + x) * S + s) : 0u;
+        }
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;   // warp = slot within the tile
@@ -214,11 +228,21 @@ __global__ void __launch_bounds__(256) bitset_to_planes_kernel(int B, int H, int
     for (int g = 0; g < kPlaneX / 32; ++g) tout[warp][lane][g] = transpose32(tin[32 * g + lane][warp], lane);
     __syncthreads();
     const int Kp = 32 * S;
-    for (int i = threadIdx.x; i < kPlaneS * 32 * (kPlaneX / 32); i += blockDim.x) {
-        const int g = i % (kPlaneX / 32), bit = (i / (kPlaneX / 32)) % 32, sl = i / (32 * (kPlaneX / 32));
-        const int s = s0 + sl, q = (x0 >> 5) + g;
-        if (s >= S || q >= WQ) continue;
-        planes[(((int64_t)b * Kp + 32 * s + bit) * H + y) * WQ + q] = tout[sl][bit][g];
+    const int q0 = x0 >> 5;
+    const int nq = min(kPlaneX / 32, WQ - q0);
+    // one plane row segment (16 words) per (slot, bit): 4 threads store 4 words each
+    for (int i = threadIdx.x; i < kPlaneS * 32 * 4; i += blockDim.x) {
+        const int quad = i & 3, bit = (i >> 2) & 31, sl = i >> 7;
+        const int s = s0 + sl;
+        if (s >= S) continue;
+        uint32_t* dst = planes + (((int64_t)b * Kp + 32 * s + bit) * H + y) * WQ + q0;
+        const uint32_t* src = tout[sl][bit];
+        const int g0 = 4 * quad;
+        if (g0 + 4 <= nq && (((uintptr_t)(dst + g0)) & 15) == 0) {
+            *(uint4*)(dst + g0) = make_uint4(src[g0], src[g0 + 1], src[g0 + 2], src[g0 + 3]);
+        } else {
+            for (int g = g0; g < g0 + 4 && g < nq; ++g) dst[g] = src[g];
+        }
     }
 }
 

@@ -33,7 +33,7 @@ constexpr int kBinThreads = 256;
 constexpr int kBinPPT = 8;
 constexpr int kChunk = kBinThreads * kBinPPT;  // primitives per bin CTA
 constexpr int kHT = 1024;                      // tile hash slots per chunk
-constexpr int kStage = 16;                     // staged entries per bin thread
+constexpr int kStage = 8;                      // staged entries per bin thread
 constexpr int kSpill = 1024;                   // shared spill entries per chunk
 constexpr int kRasterThreads = 512;
 constexpr int kMaxRun = 28;                    // fragments per entry (27 step bits)
