@@ -312,6 +312,25 @@ def backward_antialiased_cluster_bitset(frag_pix, frag_attrs_dda, bitset, target
          float(kernel_radius), float(rho), ptr(ws), ws.numel(), _stream(pos))
 
 
+def antialiased_cluster_bitset_grad_planes(bitset_planes, target_planes, shape, pos, tri, edges, edge2tri,
+                                           edge2cluster, kernel_radius, rho, d_pos=None, ws=None) -> torch.Tensor:
+    """The fused gradient from cluster planes (``bitset_to_planes``) of the bitset and the
+    target; ``shape`` = (B, H, W, S) of the bitsets."""
+    B, H, W, S = shape
+    V = pos.shape[1]
+    _arr(pos, _f32, 3, 4, "pos")
+    _cuda(bitset_planes, target_planes, pos, tri, edges, edge2tri, edge2cluster)
+    if d_pos is None:
+        d_pos = torch.zeros_like(pos)
+    need = _lib.lib().s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V, edges.shape[0])
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, pos.device)
+    call("s2c_antialiased_cluster_bitset_grad_planes", B, H, W, S, ptr(bitset_planes), ptr(target_planes), V,
+         ptr(pos), tri.shape[0], ptr(tri), edges.shape[0], ptr(edges), ptr(edge2tri), ptr(edge2cluster), ptr(d_pos),
+         float(kernel_radius), float(rho), ptr(ws), ws.numel(), _stream(pos))
+    return d_pos
+
+
 def antialiased_cluster_bitset_grad(bitset, target_bitset, pos, tri, edges, edge2tri, edge2cluster, kernel_radius,
                                     rho, d_pos=None, ws=None) -> torch.Tensor:
     """Fused silhouette marking + edge DDA + edge gradient; returns d_pos (B, V, 4), added

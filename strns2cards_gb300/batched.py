@@ -85,7 +85,7 @@ def synthetic_clusters(num_clusters=256, verts=64, min_strands=20, max_strands=2
 class BatchedClusterFit:
     """Device state of a batched fit; ``step()`` runs one iteration for every cluster."""
 
-    def __init__(self, batch: ClusterBatch, device="cuda", lr: float = 1e-4, lam: float = 0.5,
+    def __init__(self, batch: ClusterBatch, device="cuda", lr: float = 0.25, lam: float = 0.5,
                  laplacian_steps: int = 10, kernel_radius: float = 7.0, rho: float = 1.0):
         dev = torch.device(device)
         self.batch = batch
@@ -132,8 +132,10 @@ class BatchedClusterFit:
         self.d_pos.zero_()
         _core.antialiased_cluster_bitset_grad(self.bits, self.target, self.cpos, self.ctri, self.cedges, self.ce2t,
                                               self.ce2c, self.kr, self.rho, d_pos=self.d_pos, ws=self.ws_aa)
-        # gradient step on x, y, then Laplacian smoothing of every card
-        self.cpos[..., :2].sub_(self.d_pos[..., :2], alpha=self.lr)
+        # gradient step on x, y (each cluster's largest move lr pixels), then Laplacian smoothing
+        g = self.d_pos[..., :2]
+        scale = (2.0 * self.lr / max(self.H, self.W)) / g.abs().amax(dim=(1, 2), keepdim=True).clamp_min(1e-30)
+        self.cpos[..., :2].sub_(g * scale)
         self.xyz.copy_(self.cpos[..., :3].reshape(-1, 3))
         self.lap(self.xyz, self.lam, self.nlap, out=self.xyz)
         self.cpos[..., :3].copy_(self.xyz.view(self.C, -1, 3))
@@ -182,7 +184,8 @@ class BatchedClusterFit:
             d = _core.antialiased_cluster_bitset_grad(self.bits[sl], self.target[sl], self.cpos[sl].contiguous(),
                                                       self.ctri, self.cedges, self.ce2t, self.ce2c, self.kr, self.rho)
             p = self.cpos[c]
-            p[:, :2].sub_(d[0, :, :2], alpha=self.lr)
+            g = d[0, :, :2]
+            p[:, :2].sub_(g * ((2.0 * self.lr / max(self.H, self.W)) / g.abs().amax().clamp_min(1e-30)))
             xyz = p[:, :3].contiguous()
             self.lap(xyz, self.lam, self.nlap, out=xyz)
             p[:, :3].copy_(xyz)

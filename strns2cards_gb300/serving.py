@@ -1,0 +1,236 @@
+"""Continuous-batching server for strands-to-cards fitting jobs.
+
+A job is one model: its strands (clip space of the job's view), its card mesh and a
+number of fitting iterations of the full-size single-model pipeline -- card raster
+(cluster bitset), antialias forward (XOR loss) and backward, per-card IoU, a gradient
+step on the card vertices.  The server keeps every admitted job's state resident on the
+device (card positions, target bitset, workspaces) and runs each job on its own CUDA
+stream; in every scheduling round it issues one iteration of every active job, so the
+jobs' kernels overlap on the GPU.  Requests that arrive while others run wait in a queue
+and are admitted, oldest first, as soon as the HBM budget has room for their footprint;
+a finished job's memory is released before the next admission.
+
+``serve(requests, budget_bytes)`` replays a timed request stream (arrival offsets in
+seconds) and returns per-job latency (completion - arrival) and results;
+``serve_serial`` runs the same jobs one after another with the plain per-call path.
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import _core, _lib
+from .dda import dda_cluster_bitset
+from .mesh import build_edges_from_triangles
+from .rasterize import rasterize_fused
+
+
+@dataclass
+class JobSpec:
+    """Host payload of one request."""
+    strand_pos: np.ndarray     # (1, N*V, 4) float32 clip positions
+    strand_edges: np.ndarray   # (E, 2) int32
+    strand_e2c: np.ndarray     # (E,) int32
+    card_pos: np.ndarray       # (1, Vc, 4) float32
+    card_tri: np.ndarray       # (T, 3) int32
+    card_t2c: np.ndarray       # (T,) int32
+    res: int
+    clusters: int
+    iterations: int = 50
+    lr: float = 0.25          # largest vertex move per iteration, in pixels
+    arrival: float = 0.0       # seconds after the start of the stream
+    name: str = ""
+
+    def footprint(self) -> int:
+        """Device bytes the job holds while admitted (inputs, bitsets, planes, workspaces)."""
+        S = (self.clusters + 31) // 32
+        bits = self.res * self.res * S * 4
+        Vc, T = self.card_pos.shape[1], self.card_tri.shape[0]
+        E = self.strand_edges.shape[0]
+        cards = Vc * 16 * 3 + T * 16 + 3 * T * 8 + 3 * T * 4
+        return 4 * bits + 8 * self.res * self.res + 2 * cards + self.strand_pos.nbytes + E * 60 + (64 << 20)
+
+
+def synthetic_job(n_strands: int, verts: int, res: int, clusters: int, seed: int, iterations: int = 50,
+                  arrival: float = 0.0) -> JobSpec:
+    """A job of the stream: strands of the generator, one 16 x 4-quad card per cluster."""
+    from . import synthetic as syn
+    strands = syn.make_strands(n_strands, verts, seed=seed)
+    mvp = syn.ortho_cameras(strands, margin=0.3, num_views=1)
+    pos = syn.project(strands.reshape(-1, 3), mvp)
+    edges = syn.strand_edges(n_strands, verts)
+    K = min(clusters, n_strands)
+    e2c = (np.arange(edges.shape[0]) // (verts - 1) * K // n_strands).astype(np.int32)
+    cards = syn.make_cards(strands, 0, 16, 4, num_cards=K)
+    cpos = syn.project(cards.verts, mvp)
+    return JobSpec(pos, edges, e2c, cpos, cards.tri, cards.tri2cluster.astype(np.int32), res, clusters,
+                   iterations, arrival=arrival, name=f"{n_strands}x{verts}@{res}/K{clusters}")
+
+
+def step_towards(pos: torch.Tensor, d_pos: torch.Tensor, lr: float, res: int):
+    """Gradient step on the clip-space x, y of the vertices, normalised so that the largest
+    move is ``lr`` pixels (2 / res NDC units per pixel); no host synchronisation."""
+    g = d_pos[..., :2]
+    scale = (2.0 * lr / res) / g.abs().amax().clamp_min(1e-30)
+    pos[..., :2].sub_(g * scale)
+
+
+@dataclass
+class JobResult:
+    name: str
+    arrival: float
+    admitted: float = 0.0
+    finished: float = 0.0
+    card_pos: Optional[np.ndarray] = None
+    loss: List[int] = field(default_factory=list)
+    iou_inter: Optional[np.ndarray] = None
+    iou_union: Optional[np.ndarray] = None
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+class _Active:
+    """Device state of an admitted job."""
+
+    def __init__(self, spec: JobSpec, dev, stream):
+        self.spec = spec
+        self.stream = stream
+        self.done_iters = 0
+        H = W = spec.res
+        S = (spec.clusters + 31) // 32
+        L = _lib.lib()
+        with torch.cuda.stream(stream):
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().to(dev, non_blocking=True)  # noqa
+            spos, sedges, se2c = t(spec.strand_pos), t(spec.strand_edges), t(spec.strand_e2c)
+            self.cpos = t(spec.card_pos)
+            self.tri, self.t2c = t(spec.card_tri), t(spec.card_t2c)
+            edges, e2t = build_edges_from_triangles(spec.card_tri)
+            self.edges, self.e2t = t(edges), t(e2t)
+            self.e2c = t(spec.card_t2c[e2t[:, 0]].astype(np.int32))
+            self.target = dda_cluster_bitset((H, W), spos, sedges, se2c, spec.clusters)
+            del spos, sedges, se2c
+            # the target's cluster planes stay resident for the whole job
+            self.tplanes = _core.bitset_to_planes(self.target)
+            self.pplanes = torch.empty_like(self.tplanes)
+            self.bits = torch.empty((1, H, W, S), dtype=torch.int32, device=dev)
+            self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(1, H, W, self.tri.shape[0]),
+                                      dtype=torch.uint8, device=dev)
+            self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_planes_workspace_size(
+                1, self.cpos.shape[1], self.edges.shape[0]), dtype=torch.uint8, device=dev)
+            self.d_pos = torch.zeros_like(self.cpos)
+            self.losses = []
+            self.iou = None
+
+    def iterate(self):
+        spec = self.spec
+        with torch.cuda.stream(self.stream):
+            rasterize_fused((spec.res, spec.res), self.cpos, self.tri, self.t2c, spec.clusters, want_rast=False,
+                            bitset=self.bits, workspace=self.ws_tri)
+            self.losses.append(_core.xor_popcount(self.bits, self.target))
+            self.d_pos.zero_()
+            _core.bitset_to_planes(self.bits, self.pplanes)
+            _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, tuple(self.bits.shape),
+                                                         self.cpos, self.tri, self.edges, self.e2t, self.e2c, 7.0,
+                                                         0.5, d_pos=self.d_pos, ws=self.ws_aa)
+            self.iou = _core.cluster_iou_counts(self.bits, self.target, spec.clusters)
+            step_towards(self.cpos, self.d_pos, spec.lr, spec.res)
+        self.done_iters += 1
+
+    def finish(self, res: JobResult):
+        with torch.cuda.stream(self.stream):
+            res.card_pos = self.cpos.cpu().numpy()
+            res.loss = [int(x.item()) for x in self.losses]
+            res.iou_inter = self.iou[0].cpu().numpy()
+            res.iou_union = self.iou[1].cpu().numpy()
+
+
+def serve(requests: List[JobSpec], budget_bytes: int, device="cuda", max_active: int = 32,
+          realtime: bool = True) -> List[JobResult]:
+    """Continuous batching over a timed request stream; returns results in request order."""
+    dev = torch.device(device)
+    order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
+    results = [JobResult(r.name, r.arrival) for r in requests]
+    pending: List[int] = []
+    active = {}
+    used = 0
+    streams = [torch.cuda.Stream(device=dev) for _ in range(max_active)]
+    free_streams = list(range(max_active))
+    t0 = time.perf_counter()
+    nxt = 0
+    while nxt < len(order) or pending or active:
+        now = time.perf_counter() - t0
+        while nxt < len(order) and (requests[order[nxt]].arrival <= now or not realtime):
+            pending.append(order[nxt])
+            nxt += 1
+        # admit, oldest first, while the budget and the stream pool allow
+        while pending and free_streams:
+            i = pending[0]
+            need = requests[i].footprint()
+            if used + need > budget_bytes and active:
+                break
+            pending.pop(0)
+            used += need
+            sid = free_streams.pop()
+            results[i].admitted = time.perf_counter() - t0
+            active[i] = (_Active(requests[i], dev, streams[sid]), sid, need)
+        if not active:
+            if nxt < len(order):
+                time.sleep(max(0.0, min(0.005, requests[order[nxt]].arrival - now)))
+            continue
+        # one iteration of every active job, each on its own stream
+        for i, (job, sid, need) in list(active.items()):
+            job.iterate()
+        for i, (job, sid, need) in list(active.items()):
+            if job.done_iters >= job.spec.iterations:
+                job.finish(results[i])                      # synchronises the job's stream
+                results[i].finished = time.perf_counter() - t0
+                del active[i]
+                used -= need
+                free_streams.append(sid)
+                del job
+    torch.cuda.synchronize()
+    return results
+
+
+def serve_serial(requests: List[JobSpec], device="cuda", realtime: bool = True) -> List[JobResult]:
+    """The same jobs one at a time (plain calls on the default stream), in arrival order."""
+    dev = torch.device(device)
+    order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
+    results = [JobResult(r.name, r.arrival) for r in requests]
+    t0 = time.perf_counter()
+    stream = torch.cuda.current_stream(dev)
+    for i in order:
+        now = time.perf_counter() - t0
+        if realtime and requests[i].arrival > now:
+            time.sleep(requests[i].arrival - now)
+        results[i].admitted = time.perf_counter() - t0
+        job = _Active(requests[i], dev, stream)
+        for _ in range(requests[i].iterations):
+            job.iterate()
+        job.finish(results[i])
+        results[i].finished = time.perf_counter() - t0
+        del job
+    return results
+
+
+def poisson_stream(num_requests: int, rate: float = 20.0, seed: int = 1, scale: float = 1.0,
+                   iterations: int = 50) -> List[JobSpec]:
+    """Request stream: Poisson arrivals (rate per second, seed 1); strand count log-uniform in
+    [5k, 200k] x ``scale``, vertices in {32, 64, 128}, resolution in {512, 1024, 2048},
+    clusters in {256, 1024, 4096}."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=num_requests))
+    out = []
+    for k in range(num_requests):
+        n = int(np.exp(rng.uniform(np.log(5_000), np.log(200_000))) * scale)
+        v = int(rng.choice([32, 64, 128]))
+        res = int(rng.choice([512, 1024, 2048]))
+        K = int(rng.choice([256, 1024, 4096]))
+        out.append(synthetic_job(max(n, 16), v, res, K, seed=1000 + k, iterations=iterations, arrival=float(t[k])))
+    return out

@@ -28,8 +28,8 @@ def close(a, b, tol=1e-5):
 def test_batched_equals_per_cluster_and_graph_equals_eager():
     from strns2cards_gb300.batched import BatchedClusterFit, FitSchedule
     batch = small_batch()
-    fa = BatchedClusterFit(batch, lr=1e-3)
-    fb = BatchedClusterFit(batch, lr=1e-3)
+    fa = BatchedClusterFit(batch)
+    fb = BatchedClusterFit(batch)
     fb.prepare_plain()
     for _ in range(3):
         fa.eager_step()
@@ -39,8 +39,8 @@ def test_batched_equals_per_cluster_and_graph_equals_eager():
     assert close(fa.cpos, fb.cpos)
     assert not torch.equal(fa.cpos, torch.from_numpy(batch.card_pos).cuda())   # the cards moved
     # graph replay == eager
-    fc = BatchedClusterFit(batch, lr=1e-3)
-    fd = BatchedClusterFit(batch, lr=1e-3)
+    fc = BatchedClusterFit(batch)
+    fd = BatchedClusterFit(batch)
     fc.capture()
     fc.cpos.copy_(torch.from_numpy(batch.card_pos).cuda())        # undo the capture warm-up
     for _ in range(3):
@@ -48,5 +48,5 @@ def test_batched_equals_per_cluster_and_graph_equals_eager():
         fd.eager_step()
     torch.cuda.synchronize()
     assert torch.equal(fc.bits, fd.bits) and close(fc.cpos, fd.cpos, 1e-6)
-    sched = FitSchedule(BatchedClusterFit(batch, lr=1e-3), trials=2)
+    sched = FitSchedule(BatchedClusterFit(batch), trials=2)
     assert sched.best in ("eager", "eager2", "graph", "graph2") and len(sched.results) == 4
