@@ -123,6 +123,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(rows)}
 
 
+def max_over_ranks(seconds: float, ws: int, device) -> float:
+    """The slowest rank's time (all ranks get it); one rank: the value itself."""
+    if ws <= 1:
+        return seconds
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, ws: int, seconds_max: float) -> float:
+    """Units all ranks processed divided by the slowest rank's time (weak scaling)."""
+    return units_per_rank * ws / seconds_max
+
+
 def make_inputs(view):
     from strns2cards_gb300 import synthetic as syn
     sc = syn.strand_scene(NUM_STRANDS, NUM_VERTS, per_cluster=PER_CLUSTER, num_views=view + 1, seed=0)
@@ -222,42 +238,56 @@ def run_ours(args):
         dist.barrier()
     ms = [a.elapsed_time(b) for a, b in evs]
     dev_s = sum(ms) / 1e3
-    t_max = dev_s
-    if ws > 1:
-        t = torch.tensor([dev_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    segs_total = B * E * args.steps * ws
-    value = segs_total / t_max / 1e9
+    t_max = max_over_ranks(dev_s, ws, dev)
+    value = whole_job_rate(B * E * args.steps, ws, t_max) / 1e9
 
-    # e2e through the public op with host buffers (pinned), copies inside the timed region
+    # e2e through the public op with host buffers (pinned), copies inside the timed region.
+    # Steps are pipelined on three streams: the inputs of step i+1 go up while step i runs
+    # and the bitset of step i-1 comes back; every step copies its own inputs in and its
+    # whole bitset out.  Device and host buffers are double-buffered, reuse ordered by events.
     pos_p = torch.from_numpy(pos_h).pin_memory()
     edges_p = torch.from_numpy(edges_h).pin_memory()
     e2c_p = torch.from_numpy(e2c_h).pin_memory()
-    out_p = torch.empty(out.shape, dtype=torch.int32).pin_memory()
+    outs_p = [torch.empty(out.shape, dtype=torch.int32).pin_memory() for _ in range(2)]
+    dins = [(torch.empty_like(pos), torch.empty_like(edges), torch.empty_like(e2c)) for _ in range(2)]
+    douts = [out, torch.empty_like(out)]
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
     e2e_steps = max(3, min(args.steps, 10))
 
-    def e2e_step():
-        pd = pos_p.to(dev, non_blocking=True)
-        ed = edges_p.to(dev, non_blocking=True)
-        cd = e2c_p.to(dev, non_blocking=True)
-        r = s2c.dda_cluster_bitset((RES, RES), pd, ed, cd, K, out=out, workspace=work)
-        out_p.copy_(r, non_blocking=True)
+    def e2e_run(k):
+        ev_in = [torch.cuda.Event() for _ in range(k)]
+        ev_op = [torch.cuda.Event() for _ in range(k)]
+        ev_out = [torch.cuda.Event() for _ in range(k)]
+        for i in range(k):
+            pd, ed, cd = dins[i % 2]
+            with torch.cuda.stream(s_in):
+                if i >= 2:
+                    s_in.wait_event(ev_op[i - 2])
+                pd.copy_(pos_p, non_blocking=True)
+                ed.copy_(edges_p, non_blocking=True)
+                cd.copy_(e2c_p, non_blocking=True)
+                ev_in[i].record(s_in)
+            stream.wait_event(ev_in[i])
+            if i >= 2:
+                stream.wait_event(ev_out[i - 2])
+            s2c.dda_cluster_bitset((RES, RES), pd, ed, cd, K, out=douts[i % 2], workspace=work)
+            ev_op[i].record(stream)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_op[i])
+                outs_p[i % 2].copy_(douts[i % 2], non_blocking=True)
+                ev_out[i].record(s_out)
+        stream.wait_stream(s_out)
 
-    e2e_step()
+    e2e_run(2)
     torch.cuda.synchronize()
     ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ea.record(stream)
-    for _ in range(e2e_steps):
-        e2e_step()
+    s_in.wait_stream(stream)
+    e2e_run(e2e_steps)
     eb.record(stream)
     torch.cuda.synchronize()
-    e2e_s = ea.elapsed_time(eb) / 1e3
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = B * E * e2e_steps * ws / e2e_s / 1e9
+    e2e_s = max_over_ranks(ea.elapsed_time(eb) / 1e3, ws, dev)
+    e2e = whole_job_rate(B * E * e2e_steps, ws, e2e_s) / 1e9
     h2d = pos_h.nbytes + edges_h.nbytes + e2c_h.nbytes
     d2h = out.numel() * 4
 
