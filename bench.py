@@ -414,6 +414,7 @@ def wl_iteration():
     antialias forward (XOR loss) and backward, per-card IoU."""
     import torch
     import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
     from strns2cards_gb300 import synthetic as syn
     strands, mvp, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
     pos = syn.project(cards.verts, mvp)
@@ -431,24 +432,27 @@ def wl_iteration():
                                      torch.from_numpy(se2c).to(dev), 2048)
         from strns2cards_gb300 import _lib
         need = _lib.lib().s2c_rasterize_fused_workspace_size(1, H, H, T)
-        return {"tgt": tgt, "ws": torch.empty(need, dtype=torch.uint8, device=dev),
-                "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=dev),
-                "bits": torch.empty((1, H, H, 64), dtype=torch.int32, device=dev)}
+        tplanes = _core.bitset_to_planes(tgt)              # the target's planes, built once per fit
+        return {"tplanes": tplanes, "pplanes": torch.empty_like(tplanes),
+                "ws": torch.empty(need, dtype=torch.uint8, device=dev),
+                "rast": torch.empty((1, H, H, 4), dtype=torch.float32, device=dev)}
 
     def step(d, st):
-        rast, bits = s2c.rasterize_fused((H, H), d["pos"], d["tri"], d["t2c"], 2048, rast=st["rast"],
-                                         bitset=st["bits"], workspace=st["ws"])
-        loss = s2c.xor_error(bits, st["tgt"])
-        d_pos = s2c.antialiased_cluster_bitset_grad(bits, st["tgt"], d["pos"], d["tri"], d["edges"], d["e2t"],
-                                                    d["e2c"], 7.0, 0.5)
-        iou = s2c.cluster_iou(bits, st["tgt"], 2048)[1:]
-        return (rast, loss, d_pos) + tuple(iou)
+        # the whole iteration in cluster-plane layout: raster, XOR loss, antialias, IoU
+        pp = _core.rasterize_fused_planes(d["pos"], d["tri"], d["t2c"], 2048, H, H, planes=st["pplanes"],
+                                          rast=st["rast"], ws=st["ws"])
+        loss = _core.xor_popcount(pp, st["tplanes"])
+        d_pos = _core.antialiased_cluster_bitset_grad_planes(pp, st["tplanes"], (1, H, H, 64), d["pos"], d["tri"],
+                                                             d["edges"], d["e2t"], d["e2c"], 7.0, 0.5)
+        iou = _core.cluster_iou_counts_planes(pp, st["tplanes"], (1, H, H, 64), 2048)
+        return (st["rast"], loss, d_pos) + tuple(iou)
     alg = (16 * V + 12 * T + 16 * H * H + 4 * H * H * 64) + 2 * 4 * H * H * 64 + \
           (2 * 4 * H * H * 64 + 16 * V + 20 * E + 16 * V) + 2 * 4 * H * H * 64
     return dict(name="iteration", host=host, setup=setup, step=step, units=1, unit="iter/s", scale=1.0,
                 metric="plain fit iterations per second", alg_bytes=alg, launches=None,
                 workload="one fit iteration of 2,048 cards against the 50,000x100 strands' bitset, 1024x1024, "
-                         "K=2048: fused raster (rast + bitset), XOR loss, fused antialias backward, per-card IoU")
+                         "K=2048: fused raster (rast + cluster planes), XOR loss, fused antialias backward, "
+                         "per-card IoU, all in cluster-plane layout (target planes built once)")
 
 
 def wl_cluster_iou():

@@ -156,6 +156,13 @@ S2C_API s2c_status s2c_depth_test(int B, int H, int W, int64_t num_frags, const 
  * keys, the triangles' screen rectangles and the prefix of their areas (the work is split
  * evenly over the bbox pixels on the device). */
 S2C_API size_t s2c_rasterize_fused_workspace_size(int B, int H, int W, int T);
+/* new: the same pass writing cluster planes (B, 32 S, H, ceil(W / 32)) (zeroed here) instead
+ * of the (B, H, W, S) bitset -- the layout the antialias windows and the per-cluster counts
+ * read -- and rast (nullable). */
+S2C_API s2c_status s2c_rasterize_fused_planes(int B, int H, int W, int V, const float* pos, int T,
+                                              const int32_t* tri, const int32_t* tri2cluster,
+                                              int num_tri2cluster, int S, uint32_t* planes, float* rast,
+                                              void* workspace, size_t workspace_bytes, s2c_stream stream);
 S2C_API s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream);
@@ -236,6 +243,11 @@ S2C_API s2c_status s2c_cluster_iou_counts(int64_t num_pixels, int S, int K, cons
                                           const int32_t* b, uint64_t* inter, uint64_t* uni,
                                           s2c_stream stream);
 
+/* new: per-cluster counts from cluster planes of two bitsets (as s2c_cluster_iou_counts). */
+S2C_API s2c_status s2c_cluster_iou_counts_planes(int B, int H, int W, int S, int K, const uint32_t* a,
+                                                 const uint32_t* b, uint64_t* inter, uint64_t* uni,
+                                                 s2c_stream stream);
+
 /* ---------------------------------------------------------------------------------- *
  * antialiased cluster bitset loss                                                     *
  * ---------------------------------------------------------------------------------- */
@@ -272,7 +284,8 @@ S2C_API s2c_status s2c_backward_antialiased_cluster_bitset_f64(
  * fragment list and no host synchronisation (capturable in a CUDA graph).  Same
  * contributions as mark_discontinuity_edges + dda_compute_fragments + the backward above;
  * d_pos (B, V, 4) accumulated.  The workspace holds the FP64 accumulator (B*V*3 doubles)
- * and the cluster planes of both bitsets (see s2c_bitset_to_planes), read by the windows. */
+ * and the cluster planes of both bitsets (see s2c_bitset_to_planes), read by the windows.
+ * At most 2^32 - 1 silhouette fragments per call. */
 S2C_API size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S, int E);
 S2C_API s2c_status s2c_antialiased_cluster_bitset_grad(
     int B, int H, int W, int S, const int32_t* bitset, const int32_t* target, int V, const float* pos, int T,

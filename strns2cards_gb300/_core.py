@@ -428,6 +428,41 @@ def dda_cluster_bitset(pos, edges, prim2cluster, bitset, edge_ids=None, ws=None)
     return bitset
 
 
+def rasterize_fused_planes(pos, tri, tri2cluster, cluster_count, H, W, planes=None, rast=None, ws=None):
+    """Fused card raster into cluster planes (B, 32 S, H, ceil(W / 32)) int32 (and rast when
+    given); returns planes."""
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(tri2cluster, _i32, 1, name="tri2cluster")
+    _cuda(pos, tri, tri2cluster)
+    B, V = pos.shape[0], pos.shape[1]
+    S = (int(cluster_count) + 31) // 32
+    shape = (B, 32 * S, H, (W + 31) // 32)
+    if planes is None:
+        planes = torch.empty(shape, dtype=torch.int32, device=pos.device)
+    elif tuple(planes.shape) != shape or not planes.is_contiguous():
+        raise RuntimeError("rasterize_fused_planes: planes must be contiguous " + str(shape))
+    need = _lib.lib().s2c_rasterize_fused_workspace_size(B, H, W, tri.shape[0])
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, pos.device)
+    call("s2c_rasterize_fused_planes", B, H, W, V, ptr(pos), tri.shape[0], ptr(tri), ptr(tri2cluster),
+         tri2cluster.shape[0], S, ptr(planes), ptr(rast), ptr(ws), ws.numel(), _stream(pos))
+    return planes
+
+
+def cluster_iou_counts_planes(a_planes, b_planes, shape, K) -> tuple:
+    """Per-cluster (inter, union) pixel counts from cluster planes; ``shape`` = (B, H, W, S)."""
+    B, H, W, S = shape
+    _cuda(a_planes, b_planes)
+    if a_planes.shape != b_planes.shape:
+        raise RuntimeError("cluster_iou_counts_planes: planes must have the same shape.")
+    inter = torch.empty(K, dtype=torch.int64, device=a_planes.device)
+    uni = torch.empty(K, dtype=torch.int64, device=a_planes.device)
+    call("s2c_cluster_iou_counts_planes", B, H, W, S, int(K), ptr(a_planes), ptr(b_planes), ptr(inter), ptr(uni),
+         _stream(a_planes))
+    return inter, uni
+
+
 def bitset_to_planes(bitset, planes=None) -> torch.Tensor:
     """Cluster planes (B, 32 S, H, ceil(W / 32)) int32 of a bitset (B, H, W, S)."""
     _arr(bitset, _i32, 4, name="bitset")

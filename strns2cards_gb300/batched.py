@@ -109,9 +109,11 @@ class BatchedClusterFit:
                                   dtype=torch.uint8, device=dev)
         self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(C, H, W, self.ctri.shape[0]),
                                   dtype=torch.uint8, device=dev)
-        aa_need = L.s2c_antialiased_cluster_bitset_grad_workspace_size(C, self.cpos.shape[1], H, W, 1,
-                                                                         self.cedges.shape[0])
+        aa_need = L.s2c_antialiased_cluster_bitset_grad_planes_workspace_size(C, self.cpos.shape[1],
+                                                                                self.cedges.shape[0])
         self.ws_aa = torch.empty(aa_need, dtype=torch.uint8, device=dev)
+        self.pplanes = torch.empty((C, 32, H, (W + 31) // 32), dtype=torch.int32, device=dev)
+        self.tplanes = torch.empty_like(self.pplanes)
         self.lap = CardLaplacian(self.cpos.shape[1], batch.quad_edges, dev)
         self.lr, self.lam, self.nlap = float(lr), float(lam), int(laplacian_steps)
         self.kr, self.rho = float(kernel_radius), float(rho)
@@ -125,13 +127,16 @@ class BatchedClusterFit:
                            out=self.target, workspace=self.ws_dda)
 
     def _raster(self):
-        rasterize_fused((self.H, self.W), self.cpos, self.ctri, self.ct2c, 1, want_rast=False, bitset=self.bits,
-                        workspace=self.ws_tri)
+        # the cards straight into cluster planes, the layout the gradient reads
+        _core.rasterize_fused_planes(self.cpos, self.ctri, self.ct2c, 1, self.H, self.W, planes=self.pplanes,
+                                     ws=self.ws_tri)
 
     def _update(self):
         self.d_pos.zero_()
-        _core.antialiased_cluster_bitset_grad(self.bits, self.target, self.cpos, self.ctri, self.cedges, self.ce2t,
-                                              self.ce2c, self.kr, self.rho, d_pos=self.d_pos, ws=self.ws_aa)
+        _core.bitset_to_planes(self.target, self.tplanes)
+        _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, (self.C, self.H, self.W, 1),
+                                                     self.cpos, self.ctri, self.cedges, self.ce2t, self.ce2c, self.kr,
+                                                     self.rho, d_pos=self.d_pos, ws=self.ws_aa)
         # gradient step on x, y (each cluster's largest move lr pixels), then Laplacian smoothing
         g = self.d_pos[..., :2]
         scale = (2.0 * self.lr / max(self.H, self.W)) / g.abs().amax(dim=(1, 2), keepdim=True).clamp_min(1e-30)

@@ -145,9 +145,18 @@ struct AAFrag {
     int2 ev;
 };
 
+// Per-fragment set-up of antialias.cu:121-176 (edge point, half-pixel test, neighbour,
+// c01 and the window bounds); false when the fragment contributes nothing.
+struct AAPrep {
+    float fx, fy, px, py, pw, t0, t1;
+    float2 nrm;
+    int2 ev;
+    int c, c01, h0, h1, w0, w1;
+};
+
 template <bool kPlanes>
-__device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w, float axis, float t1, int e,
-                                            float2 nrm, int lane, AAFrag& o) {
+__device__ __forceinline__ bool aa_prep(const AAArgs& A, int b, int h, int w, float axis, float t1, int e, float2 nrm,
+                                        AAPrep& P) {
     const float fH = (float)A.H, fW = (float)A.W;
     if (e < 0 || e >= A.E || b < 0 || b >= A.B || h < 0 || h >= A.H || w < 0 || w >= A.W) return false;
     const float t0 = __fsub_rn(1.f, t1);
@@ -184,16 +193,85 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
         c01 = 1 - (dot > 0.f ? bit_of(A.bitset, img + (int64_t)nh * A.W + nw, A.S, c)
                              : bit_of(A.bitset, img + (int64_t)h * A.W + w, A.S, c));
     if (c01 == 0) return false;
-    // Gaussian window (antialias.cu:121-176), taps spread over the warp
     const int R = f2i(floorf(A.kr));
     const int cw = f2i(floorf(fx)), ch = f2i(floorf(fy));
-    const int h0 = max(ch - R, 0), h1 = min(ch + R, A.H - 1) + 1;
-    const int w0 = max(cw - R, 0), w1 = min(cw + R, A.W - 1) + 1;
+    P.h0 = max(ch - R, 0);
+    P.h1 = min(ch + R, A.H - 1) + 1;
+    P.w0 = max(cw - R, 0);
+    P.w1 = min(cw + R, A.W - 1) + 1;
+    P.fx = fx;
+    P.fy = fy;
+    P.px = px;
+    P.py = py;
+    P.pw = pw;
+    P.t0 = t0;
+    P.t1 = t1;
+    P.nrm = nrm;
+    P.ev = ev;
+    P.c = c;
+    P.c01 = c01;
+    return true;
+}
+
+// Gaussian window constants of antialias.cu:121-131
+struct AAWin {
+    float cc, alpha, kr2;
+};
+
+__device__ __forceinline__ AAWin aa_win(float kr) {
+    AAWin q;
+    const float sigma = __fdiv_rn(kr, 4.f);
+    q.cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
+    q.alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
+    q.kr2 = __fmul_rn(kr, kr);
+    return q;
+}
+
+// The window of one fragment evaluated by one thread from cluster planes: its rows in
+// order, each as the 1-2 plane words covering [w0, w1) of both images, visiting only the
+// pixels where they differ; Kahan FP32 sum.  Returns dc (0 when nothing contributes).
+__device__ __forceinline__ float aa_window_thread(const AAArgs& A, int b, const AAPrep& P, const AAWin& q) {
+    float sum = 0.f, comp = 0.f;
+    if (P.w1 <= P.w0) return 0.f;
+    const int64_t pbase = ((int64_t)b * 32 * A.S + P.c) * A.H;
+    const int q0 = P.w0 >> 5, q1 = (P.w1 - 1) >> 5;
+    for (int th = P.h0; th < P.h1; ++th) {
+        const uint32_t* prow = A.pplanes + (pbase + th) * A.WQ;
+        const uint32_t* trow = A.tplanes + (pbase + th) * A.WQ;
+        const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), P.fy);
+        for (int qq = q0; qq <= q1; ++qq) {
+            const int lo = max(P.w0 - 32 * qq, 0), hi = min(P.w1 - 32 * qq, 32);
+            const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+            const uint32_t pv = __ldg(prow + qq), tv = __ldg(trow + qq);
+            const uint32_t pos = pv & ~tv & m;
+            uint32_t any = (pv ^ tv) & m;
+            while (any) {
+                const int bit = __ffs(any) - 1;
+                any &= any - 1;
+                const float dx = __fsub_rn(__fadd_rn((float)(32 * qq + bit), 0.5f), P.fx);
+                const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+                if (!(n2 < q.kr2)) continue;
+                const float wgt = __fmul_rn(q.cc, expf(-q.alpha * n2));
+                kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, A.rho) : -wgt);
+            }
+        }
+    }
+    return __fmul_rn((float)P.c01, __fsub_rn(sum, comp));
+}
+
+template <bool kPlanes>
+__device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w, float axis, float t1, int e,
+                                            float2 nrm, int lane, AAFrag& o) {
+    AAPrep P;
+    if (!aa_prep<kPlanes>(A, b, h, w, axis, t1, e, nrm, P)) return false;
+    const int h0 = P.h0, h1 = P.h1, w0 = P.w0, w1 = P.w1;
+    const float fx = P.fx, fy = P.fy, px = P.px, py = P.py, pw = P.pw, t0 = P.t0;
+    const int2 ev = P.ev;
+    const int c = P.c, c01 = P.c01;
+    const int64_t img = (int64_t)b * A.H * A.W;
     const int ww = w1 - w0, taps = ww > 0 && h1 > h0 ? ww * (h1 - h0) : 0;
-    const float sigma = __fdiv_rn(A.kr, 4.f);
-    const float cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
-    const float alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
-    const float kr2 = __fmul_rn(A.kr, A.kr);
+    const AAWin q = aa_win(A.kr);
+    const float cc = q.cc, alpha = q.alpha, kr2 = q.kr2;
     // each lane sums its taps (at most ceil(taps / 32) of them) in FP32; the lanes' partial
     // sums are reduced in FP64.  Tap j = lane + 32 i sits at (row, col) = divmod(j, ww),
     // stepped incrementally.
@@ -326,14 +404,16 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
 }
 
 // Fused edge gradient.  Pass 1 (thread per (view, edge)): the mark test and the DDA span
-// count, as a number of chunks of kAAChunk fragments; a device scan; pass 2 (warp per
-// chunk): the chunk's fragments (those dda_compute_fragments + filter_valid_fragments
-// would list) through their windows read from cluster planes, the contributions summed
-// with compensation and added to the FP64 accumulator once per chunk.  Long edges spread
-// over many warps; no fragment list, no host round trip.
-constexpr int kAAChunk = 8;
+// count (the fragments dda_compute_fragments would list for the edge); a device scan;
+// pass 2: one thread per fragment.  Warps take equal chunks of the global fragment index
+// space; each lane of a warp holds one edge of a sliding window of 32 (its prefix, mark
+// normal, span and end points, computed once per edge) and every fragment takes its
+// owner's data by shuffles, regenerates its pixel with the DDA arithmetic (coverage is
+// recomputed, not stored), evaluates its window from the cluster planes and adds its
+// FP32 chain-rule contributions to the FP64 accumulator.
+constexpr int kAAFragChunk = 64;
 
-__global__ void __launch_bounds__(256) aa_chunk_count_kernel(AAArgs A, Mesh M, int32_t* __restrict__ chunks) {
+__global__ void __launch_bounds__(256) aa_count_kernel(AAArgs A, Mesh M, int32_t* __restrict__ counts) {
     const int64_t BE = (int64_t)A.B * M.E;
     for (int64_t pe = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pe < BE; pe += (int64_t)gridDim.x * blockDim.x) {
         const int b = (int)M.divE.div((uint32_t)pe);
@@ -342,72 +422,134 @@ __global__ void __launch_bounds__(256) aa_chunk_count_kernel(AAArgs A, Mesh M, i
         int n = 0;
         if (mark_edge(A.H, A.W, M, b, e, nrm) == 2) {
             const int2 ev = __ldg(M.edges + e);
-            const Span sp = dda_span(__ldg(M.pos4 + (int64_t)b * M.V + ev.x), __ldg(M.pos4 + (int64_t)b * M.V + ev.y),
-                                     A.H, A.W);
-            n = (sp.count + kAAChunk - 1) / kAAChunk;
+            n = dda_span(__ldg(M.pos4 + (int64_t)b * M.V + ev.x), __ldg(M.pos4 + (int64_t)b * M.V + ev.y), A.H,
+                         A.W).count;
         }
-        chunks[pe] = n;
+        counts[pe] = n;
     }
 }
 
-__global__ void __launch_bounds__(256) aa_chunk_kernel(AAArgs A, Mesh M, const int32_t* __restrict__ prefix,
-                                                       const int64_t* __restrict__ total) {
+// one lane's edge of the window
+struct AAEdge {
+    float4 p0, p1;
+    Span sp;
+    float2 nrm;
+    int b, e;
+};
+
+__device__ __forceinline__ void aa_load_edge(const AAArgs& A, const Mesh& M, int64_t pe, int64_t BE, AAEdge& g) {
+    g.b = 0;
+    g.e = -1;
+    g.sp.count = 0;
+    if (pe >= BE) return;
+    g.b = (int)M.divE.div((uint32_t)pe);
+    g.e = (int)pe - g.b * M.E;
+    if (mark_edge(A.H, A.W, M, g.b, g.e, g.nrm) != 2) {
+        g.e = -1;
+        return;
+    }
+    const int2 ev = __ldg(M.edges + g.e);
+    g.p0 = __ldg(M.pos4 + (int64_t)g.b * M.V + ev.x);
+    g.p1 = __ldg(M.pos4 + (int64_t)g.b * M.V + ev.y);
+    g.sp = dda_span(g.p0, g.p1, A.H, A.W);
+}
+
+__device__ __forceinline__ float4 shfl4(float4 v, int src) {
+    return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+                       __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
+}
+
+__global__ void __launch_bounds__(256) aa_frag_kernel(AAArgs A, Mesh M, const uint32_t* __restrict__ prefix,
+                                                      const int64_t* __restrict__ total) {
     const int lane = threadIdx.x & 31;
+    const int64_t BE = (int64_t)A.B * M.E;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t BE = (int64_t)A.B * M.E;
-    const int64_t nch = *total;
+    const int64_t tot64 = *total;
+    if (tot64 > 0xffffffffLL) return;   // limit: 2^32 - 1 silhouette fragments per call (header)
+    const uint32_t tot = (uint32_t)tot64;
+    const AAWin win = aa_win(A.kr);
+    const int64_t nch = ((int64_t)tot + kAAFragChunk - 1) / kAAFragChunk;
     for (int64_t ch = warp0; ch < nch; ch += nwarps) {
-        // owner edge: first pe whose inclusive prefix exceeds ch
+        const uint32_t c0 = (uint32_t)(ch * kAAFragChunk);
+        const uint32_t c1 = (uint32_t)min((int64_t)tot, (ch + 1) * kAAFragChunk);
         int64_t lo = 0, hi = BE;
         while (lo < hi) {
             const int64_t mid = (lo + hi) >> 1;
-            if ((int64_t)__ldg(prefix + mid) <= ch) lo = mid + 1;
+            if (__ldg(prefix + mid) <= c0) lo = mid + 1;
             else hi = mid;
         }
-        if (lo >= BE) continue;
-        const int64_t pe = lo;
-        const int64_t first = pe > 0 ? (int64_t)__ldg(prefix + pe - 1) : 0;
-        const int b = (int)M.divE.div((uint32_t)pe);
-        const int e = (int)pe - b * M.E;
-        float2 nrm;
-        if (mark_edge(A.H, A.W, M, b, e, nrm) != 2) continue;
-        const int2 ev = __ldg(M.edges + e);
-        const float4 p0 = __ldg(M.pos4 + (int64_t)b * M.V + ev.x), p1 = __ldg(M.pos4 + (int64_t)b * M.V + ev.y);
-        const Span sp = dda_span(p0, p1, A.H, A.W);
-        const int ee = prim_roundtrip(e);
-        const int k0 = (int)(ch - first) * kAAChunk, k1 = min(k0 + kAAChunk, sp.count);
-        float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, cmp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        bool any = false;
-        for (int k = k0; k < k1; ++k) {
+        int64_t t0 = lo;
+        uint32_t start = t0 > 0 ? __ldg(prefix + t0 - 1) : 0u;
+        uint32_t pre = t0 + lane < BE ? __ldg(prefix + t0 + lane) : 0xffffffffu;
+        AAEdge g;
+        aa_load_edge(A, M, t0 + lane, BE, g);
+        uint32_t base = c0;
+        while (base < c1) {
+            for (;;) {
+                const unsigned m = __ballot_sync(0xffffffffu, pre <= base);
+                if (!m) break;
+                const int adv = __popc(m);
+                start = __shfl_sync(0xffffffffu, pre, adv - 1);
+                t0 += adv;
+                pre = t0 + lane < BE ? __ldg(prefix + t0 + lane) : 0xffffffffu;
+                aa_load_edge(A, M, t0 + lane, BE, g);
+            }
+            const uint32_t wend = __shfl_sync(0xffffffffu, pre, 31);
+            const uint32_t end = min(min(c1, base + 32u), wend);
+            const uint32_t j = base + lane;
+            int ow = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const uint32_t pv = __shfl_sync(0xffffffffu, pre, ow + step - 1);
+                if (pv <= j) ow += step;
+            }
+            const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
+            // the owner edge's data, from its lane
+            const float4 p0 = shfl4(g.p0, ow), p1 = shfl4(g.p1, ow);
+            Span sp;
+            sp.sx = __shfl_sync(0xffffffffu, g.sp.sx, ow);
+            sp.sy = __shfl_sync(0xffffffffu, g.sp.sy, ow);
+            sp.slope = __shfl_sync(0xffffffffu, g.sp.slope, ow);
+            sp.off0 = __shfl_sync(0xffffffffu, g.sp.off0, ow);
+            sp.off1 = __shfl_sync(0xffffffffu, g.sp.off1, ow);
+            sp.axis = __shfl_sync(0xffffffffu, g.sp.axis, ow);
+            sp.count = __shfl_sync(0xffffffffu, g.sp.count, ow);
+            const float2 nrm = make_float2(__shfl_sync(0xffffffffu, g.nrm.x, ow), __shfl_sync(0xffffffffu, g.nrm.y, ow));
+            const int b = __shfl_sync(0xffffffffu, g.b, ow), e = __shfl_sync(0xffffffffu, g.e, ow);
+            base = end;
+            if (j >= end || e < 0) continue;
+            const int k = (int)(j - (ow > 0 ? prev : start));
+            if (k >= sp.count) continue;
             float x, y;
             dda_sample(sp, k, x, y);
             const int h = f2i(floorf(y)), w = f2i(floorf(x));
             if (h < 0 || h >= A.H || w < 0 || w >= A.W) continue;
             const float t1 = dda_t1(p0, p1, x, y, sp.axis, A.H, A.W);
             if (!z_ok(dda_z(p0, p1, t1))) continue;
+            const int ee = prim_roundtrip(e);
+            AAPrep P;
+            if (!aa_prep<true>(A, b, h, w, sp.axis, t1, ee, nrm, P)) continue;
             AAFrag f;
-            if (!aa_fragment<true>(A, b, h, w, sp.axis, t1, ee, nrm, lane, f)) continue;
-            if (lane != 0) continue;
+            f.dc = aa_window_thread(A, b, P, win);
+            if (f.dc == 0.f) continue;
+            f.px = P.px;
+            f.py = P.py;
+            f.pw = P.pw;
+            f.t0 = P.t0;
+            f.t1 = P.t1;
+            f.nrm = P.nrm;
+            f.ev = P.ev;
             float dpx, dpy, dpw;
             if (!aa_chain(A, f, dpx, dpy, dpw)) continue;
-            kahan_add(acc[0], cmp[0], __fmul_rn(dpx, f.t0));
-            kahan_add(acc[1], cmp[1], __fmul_rn(dpy, f.t0));
-            kahan_add(acc[2], cmp[2], __fmul_rn(dpw, f.t0));
-            kahan_add(acc[3], cmp[3], __fmul_rn(dpx, f.t1));
-            kahan_add(acc[4], cmp[4], __fmul_rn(dpy, f.t1));
-            kahan_add(acc[5], cmp[5], __fmul_rn(dpw, f.t1));
-            any = true;
-        }
-        if (lane == 0 && any) {
-            const int2 evv = __ldg(A.edges + ee);
-            double* a0 = A.acc64 + ((int64_t)b * A.V + evv.x) * 3;
-            double* a1 = A.acc64 + ((int64_t)b * A.V + evv.y) * 3;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                atomicAdd(a0 + q, (double)acc[q] - (double)cmp[q]);
-                atomicAdd(a1 + q, (double)acc[3 + q] - (double)cmp[3 + q]);
-            }
+            double* a0 = A.acc64 + ((int64_t)b * A.V + f.ev.x) * 3;
+            double* a1 = A.acc64 + ((int64_t)b * A.V + f.ev.y) * 3;
+            atomicAdd(a0 + 0, (double)__fmul_rn(dpx, f.t0));
+            atomicAdd(a0 + 1, (double)__fmul_rn(dpy, f.t0));
+            atomicAdd(a0 + 2, (double)__fmul_rn(dpw, f.t0));
+            atomicAdd(a1 + 0, (double)__fmul_rn(dpx, f.t1));
+            atomicAdd(a1 + 1, (double)__fmul_rn(dpy, f.t1));
+            atomicAdd(a1 + 2, (double)__fmul_rn(dpw, f.t1));
         }
     }
 }
@@ -607,12 +749,12 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
     A.WQ = (W + 31) / 32;
     A.kr = kernel_radius;
     A.rho = rho;
-    aa_chunk_count_kernel<<<grid_for(BE, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(A, M, ws.chunks);
-    S2C_CHECK_LAUNCH("aa_chunk_count_kernel");
+    aa_count_kernel<<<grid_for(BE, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(A, M, ws.chunks);
+    S2C_CHECK_LAUNCH("aa_count_kernel");
     s2c_status ss = inclusive_scan_i32(ws.chunks, BE, ws.prefix, ws.scan, ws.total, st);
     if (ss != S2C_OK) return ss;
-    aa_chunk_kernel<<<num_sms() * 8, 256, 0, st>>>(A, M, ws.prefix, ws.total);
-    S2C_CHECK_LAUNCH("aa_chunk_kernel");
+    aa_frag_kernel<<<num_sms() * 8, 256, 0, st>>>(A, M, (const uint32_t*)ws.prefix, ws.total);
+    S2C_CHECK_LAUNCH("aa_frag_kernel");
     aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, ws.acc, d_pos);
     S2C_CHECK_LAUNCH("aa_finalize_kernel");
     return S2C_OK;

@@ -246,6 +246,55 @@ __global__ void __launch_bounds__(256) bitset_to_planes_kernel(int B, int H, int
     }
 }
 
+// Per-cluster counts from cluster planes: one CTA per (view, plane), popcounts of a & b
+// and a | b over the plane's H * WQ contiguous words, one uint64 atomic per CTA and count.
+__global__ void __launch_bounds__(256) planes_iou_kernel(int K, int Kp, int64_t words, const uint32_t* __restrict__ a,
+                                                         const uint32_t* __restrict__ b,
+                                                         unsigned long long* __restrict__ inter,
+                                                         unsigned long long* __restrict__ uni) {
+    const int c = blockIdx.x, v = blockIdx.y;
+    if (c >= K) return;
+    const int64_t off = ((int64_t)v * Kp + c) * words;
+    const uint32_t* pa = a + off;
+    const uint32_t* pb = b + off;
+    unsigned int ni = 0, nu = 0;
+    if ((words & 3) == 0 && ((((uintptr_t)pa) | ((uintptr_t)pb)) & 15) == 0) {
+        const uint4* qa = (const uint4*)pa;
+        const uint4* qb = (const uint4*)pb;
+        for (int64_t i = threadIdx.x; i < words / 4; i += blockDim.x) {
+            const uint4 x = __ldcs(qa + i), y = __ldcs(qb + i);
+            ni += __popc(x.x & y.x) + __popc(x.y & y.y) + __popc(x.z & y.z) + __popc(x.w & y.w);
+            nu += __popc(x.x | y.x) + __popc(x.y | y.y) + __popc(x.z | y.z) + __popc(x.w | y.w);
+        }
+    } else {
+        for (int64_t i = threadIdx.x; i < words; i += blockDim.x) {
+            const uint32_t x = pa[i], y = pb[i];
+            ni += __popc(x & y);
+            nu += __popc(x | y);
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        ni += __shfl_xor_sync(0xffffffffu, ni, o);
+        nu += __shfl_xor_sync(0xffffffffu, nu, o);
+    }
+    __shared__ unsigned int si[8], su[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        si[warp] = ni;
+        su[warp] = nu;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long ti = 0, tu = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            ti += si[w];
+            tu += su[w];
+        }
+        if (ti) atomicAdd(inter + c, ti);
+        if (tu) atomicAdd(uni + c, tu);
+    }
+}
+
 }  // namespace s2c
 
 using namespace s2c;
@@ -323,5 +372,25 @@ extern "C" s2c_status s2c_bitset_to_planes(int B, int H, int W, int S, const int
     dim3 grid((unsigned)(nxt * nst), (unsigned)H, (unsigned)B);
     bitset_to_planes_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(B, H, W, S, bitset, planes);
     S2C_CHECK_LAUNCH("bitset_to_planes_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_cluster_iou_counts_planes(int B, int H, int W, int S, int K, const uint32_t* a,
+                                                    const uint32_t* b, uint64_t* inter, uint64_t* uni,
+                                                    s2c_stream stream) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && S > 0 && K >= 0 && K <= 32 * S && B <= 65535,
+                "cluster_iou_counts_planes: bad sizes");
+    S2C_REQUIRE(inter && uni, "cluster_iou_counts_planes: null output");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(inter, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(uni, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e != cudaSuccess) return cuda_status(e, "cluster_iou_counts_planes: memset");
+    if (B == 0 || H == 0 || W == 0 || K == 0) return S2C_OK;
+    S2C_REQUIRE(a && b, "cluster_iou_counts_planes: null input");
+    const int64_t words = (int64_t)H * ((W + 31) / 32);
+    planes_iou_kernel<<<dim3((unsigned)K, (unsigned)B), 256, 0, st>>>(K, 32 * S, words, a, b,
+                                                                        (unsigned long long*)inter,
+                                                                        (unsigned long long*)uni);
+    S2C_CHECK_LAUNCH("planes_iou_kernel");
     return S2C_OK;
 }

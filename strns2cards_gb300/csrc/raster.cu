@@ -200,6 +200,8 @@ struct FusedRaster {
     const int32_t* __restrict__ t2c;        // nullable
     int num_t2c;
     int32_t* __restrict__ bitset;           // nullable
+    uint32_t* __restrict__ planes;          // nullable: cluster planes (B, 32 S, H, WQ)
+    int WQ;
     unsigned long long* __restrict__ keys;  // nullable
     const int4* __restrict__ rects;         // (B*T) screen rectangles
     const uint32_t* __restrict__ prefix;    // (B*T) inclusive prefix of their areas
@@ -224,9 +226,13 @@ __device__ __forceinline__ void raster_pixel(const FusedRaster& F, const float* 
         const float zz = __fadd_rn(z, 2.f);
         atomicMin(F.keys + pix, ((unsigned long long)(uint32_t)__float_as_int(zz) << 32) | (uint32_t)ot);
     }
-    if (F.bitset && ot < F.num_t2c) {
+    if ((F.bitset || F.planes) && ot < F.num_t2c) {
         const int c = __ldg(F.t2c + ot);
-        if (c >= 0 && c < 32 * F.S) atomicOr(F.bitset + pix * F.S + (c >> 5), (int32_t)(1u << (c & 31)));
+        if (c >= 0 && c < 32 * F.S) {
+            if (F.bitset) atomicOr(F.bitset + pix * F.S + (c >> 5), (int32_t)(1u << (c & 31)));
+            if (F.planes)
+                atomicOr(F.planes + (((int64_t)ob * 32 * F.S + c) * F.H + y) * F.WQ + (x >> 5), 1u << (x & 31));
+        }
     }
 }
 
@@ -695,13 +701,35 @@ extern "C" size_t s2c_rasterize_fused_workspace_size(int B, int H, int W, int T)
     return raster_carve(B, H, W, T, true, nullptr, (size_t)-1, nullptr) + 256;
 }
 
+static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
+                                       const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
+                                       uint32_t* planes, float* rast, void* workspace, size_t workspace_bytes,
+                                       s2c_stream stream);
+
 extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                           const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                           float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream) {
+    return rasterize_fused_impl(B, H, W, V, pos, T, tri, tri2cluster, num_tri2cluster, S, bitset, nullptr, rast,
+                                workspace, workspace_bytes, stream);
+}
+
+extern "C" s2c_status s2c_rasterize_fused_planes(int B, int H, int W, int V, const float* pos, int T,
+                                                 const int32_t* tri, const int32_t* tri2cluster, int num_tri2cluster,
+                                                 int S, uint32_t* planes, float* rast, void* workspace,
+                                                 size_t workspace_bytes, s2c_stream stream) {
+    return rasterize_fused_impl(B, H, W, V, pos, T, tri, tri2cluster, num_tri2cluster, S, nullptr, planes, rast,
+                                workspace, workspace_bytes, stream);
+}
+
+static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
+                                       const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
+                                       uint32_t* planes, float* rast, void* workspace, size_t workspace_bytes,
+                                       s2c_stream stream) {
     S2C_REQUIRE(B > 0 && H > 0 && W > 0 && H <= 32768 && W <= 32768 && V >= 0 && T >= 0,
                 "rasterize_fused: bad sizes");
     S2C_REQUIRE((int64_t)B * T < (1LL << 31), "rasterize_fused: B*T too large");
-    S2C_REQUIRE(!bitset || (S > 0 && (tri2cluster || num_tri2cluster == 0)), "rasterize_fused: bitset needs S and tri2cluster");
+    S2C_REQUIRE((!bitset && !planes) || (S > 0 && (tri2cluster || num_tri2cluster == 0)),
+                "rasterize_fused: bitset needs S and tri2cluster");
     S2C_REQUIRE(pos && (T == 0 || tri), "rasterize_fused: null input");
     S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && (!rast || ((uintptr_t)rast & 15) == 0), "rasterize_fused: misaligned");
     const int64_t npix = (int64_t)B * H * W;
@@ -718,6 +746,11 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
         cudaError_t e = cudaMemsetAsync(bitset, 0, (size_t)npix * S * 4, st);
         if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset bitset");
     }
+    const int WQ = (W + 31) / 32;
+    if (planes) {
+        cudaError_t e = cudaMemsetAsync(planes, 0, (size_t)B * 32 * S * H * WQ * 4, st);
+        if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset planes");
+    }
     Tris R;
     R.pos4 = (const float4*)pos;
     R.tri = tri;
@@ -725,7 +758,7 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
     R.T = T;
     R.divT = FastDiv((uint32_t)(T > 0 ? T : 1));
     const int64_t BT = (int64_t)B * T;
-    if (BT > 0 && (rast || bitset)) {
+    if (BT > 0 && (rast || bitset || planes)) {
         tri_rect_area_kernel<<<grid_for(BT, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(H, W, B, R, ws.rects,
                                                                                            ws.areas);
         S2C_CHECK_LAUNCH("tri_rect_area_kernel");
@@ -740,6 +773,8 @@ extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const floa
         F.t2c = tri2cluster;
         F.num_t2c = num_tri2cluster;
         F.bitset = bitset;
+        F.planes = planes;
+        F.WQ = WQ;
         F.keys = ws.keys;
         F.rects = ws.rects;
         F.prefix = (const uint32_t*)ws.prefix;

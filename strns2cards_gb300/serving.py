@@ -3,8 +3,10 @@
 A job is one model: its strands (clip space of the job's view), its card mesh and a
 number of fitting iterations of the full-size single-model pipeline -- card raster
 (cluster bitset), antialias forward (XOR loss) and backward, per-card IoU, a gradient
-step on the card vertices.  The server keeps every admitted job's state resident on the
-device (card positions, target bitset, workspaces) and runs each job on its own CUDA
+step on the card vertices.  The iteration runs in cluster-plane layout (the raster writes
+planes, the loss, gradient and IoU read them).  The server keeps every admitted job's
+state resident on the device (card positions, the target's planes, workspaces) and runs
+each job on its own CUDA
 stream; in every scheduling round it issues one iteration of every active job, so the
 jobs' kernels overlap on the GPU.  Requests that arrive while others run wait in a queue
 and are admitted, oldest first, as soon as the HBM budget has room for their footprint;
@@ -52,7 +54,7 @@ class JobSpec:
         Vc, T = self.card_pos.shape[1], self.card_tri.shape[0]
         E = self.strand_edges.shape[0]
         cards = Vc * 16 * 3 + T * 16 + 3 * T * 8 + 3 * T * 4
-        return 4 * bits + 8 * self.res * self.res + 2 * cards + self.strand_pos.nbytes + E * 60 + (64 << 20)
+        return 3 * bits + 8 * self.res * self.res + 2 * cards + self.strand_pos.nbytes + E * 60 + (64 << 20)
 
 
 def synthetic_job(n_strands: int, verts: int, res: int, clusters: int, seed: int, iterations: int = 50,
@@ -117,8 +119,9 @@ class _Active:
             del spos, sedges, se2c
             # the target's cluster planes stay resident for the whole job
             self.tplanes = _core.bitset_to_planes(self.target)
+            del self.target
             self.pplanes = torch.empty_like(self.tplanes)
-            self.bits = torch.empty((1, H, W, S), dtype=torch.int32, device=dev)
+            self.shape = (1, H, W, S)
             self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(1, H, W, self.tri.shape[0]),
                                       dtype=torch.uint8, device=dev)
             self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_planes_workspace_size(
@@ -130,15 +133,15 @@ class _Active:
     def iterate(self):
         spec = self.spec
         with torch.cuda.stream(self.stream):
-            rasterize_fused((spec.res, spec.res), self.cpos, self.tri, self.t2c, spec.clusters, want_rast=False,
-                            bitset=self.bits, workspace=self.ws_tri)
-            self.losses.append(_core.xor_popcount(self.bits, self.target))
+            # the iteration in cluster-plane layout (the target's planes were built at admission)
+            _core.rasterize_fused_planes(self.cpos, self.tri, self.t2c, spec.clusters, spec.res, spec.res,
+                                         planes=self.pplanes, ws=self.ws_tri)
+            self.losses.append(_core.xor_popcount(self.pplanes, self.tplanes))
             self.d_pos.zero_()
-            _core.bitset_to_planes(self.bits, self.pplanes)
-            _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, tuple(self.bits.shape),
-                                                         self.cpos, self.tri, self.edges, self.e2t, self.e2c, 7.0,
-                                                         0.5, d_pos=self.d_pos, ws=self.ws_aa)
-            self.iou = _core.cluster_iou_counts(self.bits, self.target, spec.clusters)
+            _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, self.shape, self.cpos, self.tri,
+                                                         self.edges, self.e2t, self.e2c, 7.0, 0.5, d_pos=self.d_pos,
+                                                         ws=self.ws_aa)
+            self.iou = _core.cluster_iou_counts_planes(self.pplanes, self.tplanes, self.shape, spec.clusters)
             step_towards(self.cpos, self.d_pos, spec.lr, spec.res)
         self.done_iters += 1
 

@@ -47,6 +47,6 @@ def test_batched_equals_per_cluster_and_graph_equals_eager():
         fc.graph.replay()
         fd.eager_step()
     torch.cuda.synchronize()
-    assert torch.equal(fc.bits, fd.bits) and close(fc.cpos, fd.cpos, 1e-6)
+    assert torch.equal(fc.pplanes, fd.pplanes) and close(fc.cpos, fd.cpos, 1e-6)
     sched = FitSchedule(BatchedClusterFit(batch), trials=2)
     assert sched.best in ("eager", "eager2", "graph", "graph2") and len(sched.results) == 4

@@ -237,3 +237,23 @@ def test_rasterize_fused_ties_and_perspective():
     assert np.array_equal(np_(fr), orast)
     ofp, ofa = O.compute_fragments(H, W, pos, tri)
     assert np.array_equal(np_(fb), O.cluster_mask_from_fragments(H, W, ofp, ofa, t2c, 40, B=B))
+
+
+def test_raster_into_planes_and_plane_iou():
+    """The fused raster writing cluster planes gives the planes of the bitset it writes, and
+    the per-cluster counts from planes equal those from the bitsets."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    d = golden("tri_cards.npz")
+    H, W, K = int(d["H"]), int(d["W"]), int(d["K"])
+    pos, tri, t2c = cu(d["pos"]), cu(d["tri"]), cu(d["tri2cluster"])
+    rast, bits = s2c.rasterize_fused((H, W), pos, tri, t2c, K)
+    rast2 = torch.empty_like(rast)
+    planes = _core.rasterize_fused_planes(pos, tri, t2c, K, H, W, rast=rast2)
+    assert torch.equal(planes, _core.bitset_to_planes(bits)) and torch.equal(rast2, rast)
+    other = torch.roll(bits, 3, dims=2).contiguous()
+    op = _core.bitset_to_planes(other)
+    i1, u1 = _core.cluster_iou_counts(bits, other, K)
+    i2, u2 = _core.cluster_iou_counts_planes(planes, op, tuple(bits.shape), K)
+    assert torch.equal(i1, i2) and torch.equal(u1, u2)
+    assert int(_core.xor_popcount(planes, op)) == int(_core.xor_popcount(bits, other))
