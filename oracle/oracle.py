@@ -42,7 +42,7 @@ _SIGS = {
     "or_dda_interpolate_backward": ([I, I, I, f32p, I, f32p, i32p, f64p], None),
     "or_mark_edges": ([I, I, I, I, f32p, i32p, I, i32p, i32p, i32p, f32p], None),
     "or_compact_ints": ([I64, i32p, i32p], I64),
-    "or_aa_backward": ([I64, i32p, f32p, I, I, I, i32p, i32p, I, f32p, I, i32p, f32p, i32p, f64p, F, F], None),
+    "or_aa_backward": ([I64, i32p, f32p, I, I, I, i32p, i32p, I, f32p, I, i32p, f32p, i32p, f64p, F, F, f64p], None),
     "or_popcount": ([I64, I, i32p, f32p], None),
     "or_accumulate_rgb": ([I64, I, i32p, f32p, f32p], None),
     "or_smooth_strands": ([I, I, f32p, f32p, f64p, F], None),
@@ -258,7 +258,7 @@ def mark_discontinuity_edges(H, W, pos, tri, edges, edge2tri, raw=False):
 
 
 def aa_backward(frag_pix, frag_attrs, bitset, target, pos, edges, normals, edge2cluster,
-                kernel_radius=7.0, rho=1.0):
+                kernel_radius=7.0, rho=1.0, return_dc=False):
     fp, fa = _i32(frag_pix), _f32(frag_attrs)
     bits, tgt = _i32(bitset), _i32(target)
     pos, edges, normals, e2c = _f32(pos), _i32(edges), _f32(normals), _i32(edge2cluster)
@@ -266,10 +266,11 @@ def aa_backward(frag_pix, frag_attrs, bitset, target, pos, edges, normals, edge2
     V = pos.shape[1]
     E = edges.shape[0]
     d = np.zeros(pos.shape, np.float64)
+    dc = np.zeros(fp.shape[0], np.float64)
     lib().or_aa_backward(fp.shape[0], _p(fp, i32p), _p(fa, f32p), H, W, S, _p(bits, i32p), _p(tgt, i32p),
                          V, _p(pos, f32p), E, _p(edges, i32p), _p(normals, f32p), _p(e2c, i32p),
-                         _p(d, f64p), float(kernel_radius), float(rho))
-    return d
+                         _p(d, f64p), float(kernel_radius), float(rho), _p(dc, f64p))
+    return (d, dc) if return_dc else d
 
 
 def antialias_grad(bitset, target, pos, tri, edges, edge2tri, edge2cluster, kernel_radius=7.0, rho=1.0):

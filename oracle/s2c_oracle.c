@@ -539,9 +539,11 @@ static double adjoint_sum(int b, float x, float y, int c, int H, int W, int S,
 void or_aa_backward(int64_t F, const int32_t* frag_pix, const float* frag_attrs, int H, int W,
                     int S, const int32_t* bitset, const int32_t* target, int V,
                     const float* pos, int E, const int32_t* edges, const float* normals,
-                    const int32_t* edge2cluster, double* d_pos, float kernel_radius, float rho) {
+                    const int32_t* edge2cluster, double* d_pos, float kernel_radius, float rho,
+                    double* frag_dc) {
     const float fH = (float)H, fW = (float)W;
     for (int64_t i = 0; i < F; ++i) {
+        if (frag_dc) frag_dc[i] = 0.0;
         const int b = frag_pix[3 * i], h = frag_pix[3 * i + 1], w = frag_pix[3 * i + 2];
         const float axis = frag_attrs[4 * i], t1 = frag_attrs[4 * i + 1], t0 = 1.f - t1;
         const int e = f2i(frag_attrs[4 * i + 3]) - 1;
@@ -578,6 +580,7 @@ void or_aa_backward(int64_t F, const int32_t* frag_pix, const float* frag_attrs,
         if (c01 == 0.0) continue;
         const double dc = c01 * adjoint_sum(b, fx, fy, c, H, W, S, bitset, target, kernel_radius, rho);
         if (dc == 0.0) continue;
+        if (frag_dc) frag_dc[i] = dc;
         const double dx = dc * 0.5 * fW * nx;
         const double dy = dc * -0.5 * fH * ny;
         const double dpx = dx / pw, dpy = dy / pw;

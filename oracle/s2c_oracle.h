@@ -91,7 +91,8 @@ int64_t or_compact_ints(int64_t N, const int32_t* in, int32_t* out);
 void or_aa_backward(int64_t F, const int32_t* frag_pix, const float* frag_attrs, int H, int W,
                     int S, const int32_t* bitset, const int32_t* target, int V,
                     const float* pos, int E, const int32_t* edges, const float* normals,
-                    const int32_t* edge2cluster, double* d_pos, float kernel_radius, float rho);
+                    const int32_t* edge2cluster, double* d_pos, float kernel_radius, float rho,
+                    double* frag_dc);
 
 /* ---- bitset utils (bitset_utils.cu) ---------------------------------------------- */
 void or_popcount(int64_t npix, int S, const int32_t* bitset, float* out);
