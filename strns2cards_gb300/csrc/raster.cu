@@ -91,12 +91,14 @@ __device__ __forceinline__ bool tri_finish(const TriEdges& e, float4 P0, float4 
     const float invA = __fdiv_rn(1.f, e.A);
     b0 = __fmul_rn(e.A0, invA);
     b1 = __fmul_rn(e.A1, invA);
+    // the barycentric half of the acceptance test first: the depth division only for
+    // pixels that pass it (the conjunction, and so the result, is the same)
+    if (!isfinite(b0) || !isfinite(b1) || b0 < 0.f || b1 < 0.f || __fadd_rn(b0, b1) > 1.f) return false;
     // (A0 z0 + A1 z1) + A2 z2 and the same for w, with the reference build's fusion shapes
     const float zc = __fmaf_rn(e.A2, P2.z, __fmaf_rn(e.A1, P1.z, __fmul_rn(e.A0, P0.z)));
     const float wc = __fmaf_rn(e.A2, P2.w, __fmaf_rn(e.A0, P0.w, __fmul_rn(e.A1, P1.w)));
     z = __fdiv_rn(zc, wc);
-    if (!isfinite(b0) || !isfinite(b1) || !isfinite(z)) return false;
-    if (b0 < 0.f || b1 < 0.f || __fadd_rn(b0, b1) > 1.f || z < -1.f || z > 1.f) return false;
+    if (!isfinite(z) || z < -1.f || z > 1.f) return false;
     return true;
 }
 
