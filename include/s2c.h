@@ -328,6 +328,29 @@ S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float*
                                 const float* R, float* skinned_strands, float beta,
                                 s2c_stream stream);
 
+/* replaces: load_strands (pystrns2cards.cpp:788-816; hair_loader.cpp:15-259).  Host.
+ * Reads a .bin, .data (USC) or .hair (CY-HAIR / ZJU) file; *handle receives the strands
+ * with at least two points (counts in *num_strands, total points in *num_points), to be
+ * copied out and released by s2c_strands_take.  An unopenable file gives no strands (as
+ * the reference); a truncated one is S2C_ERR_INVALID. */
+S2C_API s2c_status s2c_load_strands(const char* path, void** handle, int64_t* num_strands, int64_t* num_points);
+S2C_API s2c_status s2c_strands_take(void* handle, int32_t* num_samples, float* points);
+
+/* replaces: resample_strands_by_arclength (pystrns2cards.cpp:818-839; hair_loader.cpp:261-307).
+ * Host: points (sum(num_samples), 3) -> out (num_strands, target, 3), the reference's FP32
+ * operations; strands need at least 2 points. */
+S2C_API s2c_status s2c_resample_strands_by_arclength_host(int num_strands, const int32_t* num_samples,
+                                                         const float* points, int target, float* out);
+
+/* new: the same on the device, one thread per strand with the same FP32 operations (results
+ * identical to the host version).  Strands with fewer than 2 points, or counts that
+ * overrun num_points, give NaN rows. */
+S2C_API size_t s2c_resample_strands_workspace_size(int num_strands, int64_t num_points);
+S2C_API s2c_status s2c_resample_strands_by_arclength(int num_strands, const int32_t* num_samples,
+                                                     const float* points, int64_t num_points, int target,
+                                                     float* out, void* workspace, size_t workspace_bytes,
+                                                     s2c_stream stream);
+
 /* ---------------------------------------------------------------------------------- *
  * card mesh topology (host)                                                           *
  * ---------------------------------------------------------------------------------- */

@@ -21,10 +21,12 @@ for u in dda rasterize antialias bitset_utils compact_utils curve_utils; do
     pids+=($!)
   fi
 done
-# the reference's host edge builder (mesh_utils.cpp) behind a small C shim, for the CPU tests
+# the reference's host edge builder and strand loader/resampler (mesh_utils.cpp,
+# hair_loader.cpp) behind a small C shim, for the CPU tests
 HERE="$(cd "$(dirname "$0")" && pwd)"
 if [ ! -f "$OUT/libref_mesh.so" ] || [ "$SRC/mesh_utils.cpp" -nt "$OUT/libref_mesh.so" ] || [ "$HERE/ref_mesh_shim.cpp" -nt "$OUT/libref_mesh.so" ]; then
-  ( g++ -O2 -std=c++17 -shared -fPIC -I"$SRC" -o "$OUT/libref_mesh.so" "$SRC/mesh_utils.cpp" "$HERE/ref_mesh_shim.cpp" ) &
+  ( g++ -O2 -std=c++17 -shared -fPIC -I"$SRC" -o "$OUT/libref_mesh.so" "$SRC/mesh_utils.cpp" "$SRC/hair_loader.cpp" \
+        "$HERE/ref_mesh_shim.cpp" ) &
   pids+=($!)
 fi
 for p in "${pids[@]}"; do wait "$p"; done

@@ -549,3 +549,44 @@ def skinning(strands, arclength, handle_strands, canonical_handles, R, skinned_s
         raise RuntimeError("skinning: skinned_strands must match (num_strands, num_points, 3).")
     call("s2c_skinning", N, V, ptr(strands), ptr(arclength), ptr(handle_strands), ptr(canonical_handles), ptr(R),
          ptr(skinned_strands), float(beta), _stream(strands))
+
+
+# ---- strand ingest (pystrns2cards.cpp:788-839) -----------------------------------------
+def load_strands(filepath):
+    """Host: (num_samples int32 (N, 1), points float32 (P, 3)) of a .bin/.data/.hair file."""
+    import numpy as np
+    h = ctypes.c_void_p()
+    n, p = _lib.i64_out(), _lib.i64_out()
+    call("s2c_load_strands", str(filepath).encode(), ctypes.byref(h), ctypes.byref(n), ctypes.byref(p),
+         exc=ValueError)
+    counts = np.empty((int(n.value), 1), np.int32)
+    points = np.empty((int(p.value), 3), np.float32)
+    call("s2c_strands_take", h, counts.ctypes.data, points.ctypes.data)
+    return counts, points
+
+
+def resample_strands_by_arclength(num_samples, points, target_num_samples):
+    """Host: (N, target, 3) float32 of ragged strands resampled uniformly in arclength."""
+    import numpy as np
+    ns = np.ascontiguousarray(num_samples, dtype=np.int32).ravel()
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    if int(ns.sum()) != pts.shape[0]:
+        raise RuntimeError("resample_strands_by_arclength: num_samples do not add up to the points.")
+    out = np.empty((ns.shape[0], int(target_num_samples), 3), np.float32)
+    call("s2c_resample_strands_by_arclength_host", ns.shape[0], ns.ctypes.data, pts.ctypes.data,
+         int(target_num_samples), out.ctypes.data)
+    return out
+
+
+def resample_strands_by_arclength_device(num_samples, points, target_num_samples, out=None):
+    """Device: the same from CUDA tensors num_samples int32 (N,) and points float32 (P, 3)."""
+    _arr(num_samples, _i32, 1, name="num_samples")
+    _arr(points, _f32, 2, 3, "points")
+    _cuda(num_samples, points)
+    N, P, T = num_samples.shape[0], points.shape[0], int(target_num_samples)
+    if out is None:
+        out = torch.empty((N, T, 3), dtype=_f32, device=points.device)
+    ws = workspace(_lib.lib().s2c_resample_strands_workspace_size(N, P), points.device)
+    call("s2c_resample_strands_by_arclength", N, ptr(num_samples), ptr(points), P, T, ptr(out), ptr(ws), ws.numel(),
+         _stream(points))
+    return out

@@ -75,6 +75,11 @@ SIGNATURES = {
     "s2c_smooth_strands": ([c_i, c_i, vp, vp, vp, c_f, vp], c_i),
     "s2c_skinning": ([c_i, c_i, vp, vp, vp, vp, vp, vp, c_f, vp], c_i),
     "s2c_build_edges_from_triangles": ([c_i, vp, vp, vp, i64p], c_i),
+    "s2c_load_strands": ([ctypes.c_char_p, ctypes.POINTER(vp), i64p, i64p], c_i),
+    "s2c_strands_take": ([vp, vp, vp], c_i),
+    "s2c_resample_strands_by_arclength_host": ([c_i, vp, vp, c_i, vp], c_i),
+    "s2c_resample_strands_workspace_size": ([c_i, c_i64], c_sz),
+    "s2c_resample_strands_by_arclength": ([c_i, vp, vp, c_i64, c_i, vp, vp, c_sz, vp], c_i),
     "s2c_build_vertex_adjacency": ([c_i, c_i, vp, vp, vp, i64p], c_i),
     "s2c_card_laplacian_smooth": ([c_i, c_i, vp, vp, c_i, vp, vp, c_f, c_i, vp], c_i),
     "s2c_lbs_bind_workspace_size": ([c_i64, c_i], c_sz),

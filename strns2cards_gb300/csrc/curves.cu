@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "scan.cuh"
 
 namespace s2c {
 namespace {
@@ -190,6 +191,54 @@ s2c_status launch_curves(bool skin, int N, int V, const float* x, const float* a
     return S2C_OK;
 }
 
+// Arclength resampling of ragged strands (the reference's host resample_strands_by_arclength,
+// hair_loader.cpp:261-307), one thread per strand with the same FP32 operations in the same
+// order: bit-identical to the host version.  ends = inclusive prefix of the point counts.
+__global__ void resample_kernel(int ns, const int32_t* __restrict__ counts, const int32_t* __restrict__ ends,
+                                const float* __restrict__ pts, int64_t npts, int T, float* __restrict__ len,
+                                float* __restrict__ out, int32_t* __restrict__ bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+        const int N = counts[i];
+        const int64_t at = (int64_t)ends[i] - N;
+        float* o = out + (int64_t)i * T * 3;
+        if (N < 2 || at < 0 || at + N > npts) {   // too short, or counts overrunning the points
+            atomicMax(bad, 1);
+            for (int k = 0; k < 3 * T; ++k) o[k] = __int_as_float(0x7fc00000);
+            continue;
+        }
+        const float* p = pts + 3 * at;
+        float* L = len + at;
+        L[0] = 0.f;
+        for (int j = 1; j < N; ++j) {
+            const float dx = __fsub_rn(p[3 * j], p[3 * j - 3]);
+            const float dy = __fsub_rn(p[3 * j + 1], p[3 * j - 2]);
+            const float dz = __fsub_rn(p[3 * j + 2], p[3 * j - 1]);
+            L[j] = __fadd_rn(L[j - 1], __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)),
+                                                           __fmul_rn(dz, dz))));
+        }
+        const float total = L[N - 1];
+        for (int j = 0; j < N; ++j) L[j] = __fdiv_rn(L[j], total);
+        for (int j = 0; j + 1 < T; ++j) {
+            const float t = __fdiv_rn((float)j, (float)(T - 1));
+            int lo = 0, hi = N;   // first index with L > t
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (!(t < L[mid])) lo = mid + 1;
+                else hi = mid;
+            }
+            const int k = min(max(lo, 1), N - 1);
+            const float den = __fsub_rn(L[k], L[k - 1]);
+            const float t0 = __fdiv_rn(__fsub_rn(L[k], t), den);
+            const float t1 = __fdiv_rn(__fsub_rn(t, L[k - 1]), den);
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                o[3 * j + c] = __fadd_rn(__fmul_rn(t0, p[3 * (k - 1) + c]), __fmul_rn(t1, p[3 * k + c]));
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[3 * (T - 1) + c] = p[3 * (N - 1) + c];
+    }
+}
+
 }  // namespace
 }  // namespace s2c
 
@@ -221,3 +270,36 @@ S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float*
 }
 
 }  // extern "C"
+
+extern "C" size_t s2c_resample_strands_workspace_size(int num_strands, int64_t num_points) {
+    const size_t ns = (size_t)(num_strands > 0 ? num_strands : 1);
+    return s2c::align_up(ns * 4, 256) + s2c::align_up((size_t)(num_points > 0 ? num_points : 1) * 4, 256) + 256 +
+           s2c::align_up(s2c::scan_workspace_bytes(ns), 256) + 512;
+}
+
+extern "C" s2c_status s2c_resample_strands_by_arclength(int num_strands, const int32_t* num_samples,
+                                                        const float* points, int64_t num_points, int target,
+                                                        float* out, void* workspace, size_t workspace_bytes,
+                                                        s2c_stream stream) {
+    S2C_REQUIRE(num_strands >= 0 && num_points >= 0 && target >= 2, "resample_strands_by_arclength: bad sizes");
+    S2C_REQUIRE(num_points < (1LL << 31), "resample_strands_by_arclength: too many points");
+    if (num_strands == 0) return S2C_OK;
+    S2C_REQUIRE(num_samples && points && out && workspace, "resample_strands_by_arclength: null pointer");
+    S2C_REQUIRE(workspace_bytes >= s2c_resample_strands_workspace_size(num_strands, num_points),
+                "resample_strands_by_arclength: workspace too small");
+    s2c::Carver cv(workspace, workspace_bytes);
+    int32_t* ends = cv.take<int32_t>(num_strands);
+    float* len = cv.take<float>(num_points > 0 ? num_points : 1);
+    int32_t* bad = cv.take<int32_t>(1);
+    void* scan = cv.take<char>(s2c::scan_workspace_bytes(num_strands));
+    int64_t* tot = cv.take<int64_t>(1);
+    cudaStream_t st = (cudaStream_t)stream;
+    s2c_status s = s2c::inclusive_scan_i32(num_samples, num_strands, ends, scan, tot, st);
+    if (s != S2C_OK) return s;
+    cudaError_t e = cudaMemsetAsync(bad, 0, 4, st);
+    if (e != cudaSuccess) return s2c::cuda_status(e, "resample_strands_by_arclength: memset");
+    s2c::resample_kernel<<<s2c::grid_for(num_strands, 128, (int64_t)s2c::num_sms() * 16), 128, 0, st>>>(
+        num_strands, num_samples, ends, points, num_points, target, len, out, bad);
+    S2C_CHECK_LAUNCH("resample_kernel");
+    return S2C_OK;
+}

@@ -100,3 +100,21 @@ def test_curves_empty_and_errors():
     with pytest.raises(ValueError):
         s2c.skinning(torch.zeros((4, 10, 3), device="cuda"), torch.zeros((4, 10, 3), device="cuda"),
                      torch.zeros((4, 10, 3), device="cuda"), torch.zeros((4, 10, 3), device="cuda"), 0.1)
+
+
+def test_device_resampling_equals_host():
+    """Ragged strands resampled on the device equal the host version bit for bit (the same
+    FP32 operations in the same order); strands too short give NaN rows."""
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(9)
+    counts = rng.integers(2, 300, size=5000).astype(np.int32)
+    pts = np.cumsum(rng.normal(scale=0.02, size=(int(counts.sum()), 3)), 0).astype(np.float32)
+    for T in (2, 33, 100):
+        host = s2c.resample_strands_by_arclength(counts, pts, T)
+        dev = s2c.resample_strands_by_arclength(cu(counts), cu(pts), T)
+        assert np.array_equal(np_(dev), host)
+    bad = counts.copy()
+    bad[7] = 1
+    bad[8] += 1
+    out = np_(s2c.resample_strands_by_arclength(cu(bad), cu(pts), 10))
+    assert np.isnan(out[7]).all()
