@@ -673,7 +673,62 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
-WORKLOADS = {"tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
+def wl_resample():
+    """Arclength resampling of 100,000 ragged strands (50..200 points, seed 0) to 100 points."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    rng = np.random.default_rng(0)
+    counts = rng.integers(50, 201, size=100_000).astype(np.int32)
+    pts = np.cumsum(rng.normal(scale=0.02, size=(int(counts.sum()), 3)), 0).astype(np.float32)
+    host = {"counts": counts, "points": pts}
+
+    def setup(d):
+        t0 = time.perf_counter()
+        _core.resample_strands_by_arclength(counts, pts, 100)      # the host path, for the record
+        return {"host_s": time.perf_counter() - t0}
+
+    def step(d, st):
+        return _core.resample_strands_by_arclength_device(d["counts"], d["points"], 100)
+    n = counts.shape[0]
+    return dict(name="resample", host=host, setup=setup, step=step, units=n, unit="Mstrands/s", scale=1e6,
+                metric="strands resampled by arclength per second (device)",
+                alg_bytes=4 * n + 12 * int(counts.sum()) + 12 * 100 * n, launches=4,
+                workload="resample_strands_by_arclength of 100,000 strands with 50..200 points to 100 points")
+
+
+def wl_msaa():
+    """Software-MSAA render of one wisp (400 strands x 64 points as a tube of 8 sides:
+    204,800 vertices, 403,200 triangles) into a 512 x 256 patch, 64 jittered samples."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    verts, faces, attr = syn.wisp_patch(400, 64, n_circle=8, seed=0)
+    offsets, weights = s2c.msaa_pattern(8)
+    H, W = 512, 256
+    host = {"pos": verts, "tri": faces, "attr": attr}
+
+    def setup(d):
+        # the reference's per-sample loop over the drop-in ops, timed for the record
+        s2c.msaa_render_loop((H, W), d["pos"], d["tri"], d["attr"], offsets, weights)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        s2c.msaa_render_loop((H, W), d["pos"], d["tri"], d["attr"], offsets, weights)
+        b.record()
+        torch.cuda.synchronize()
+        return {"config_extra": {"per_sample_loop_ms": a.elapsed_time(b)}}
+
+    def step(d, st):
+        return s2c.msaa_render((H, W), d["pos"], d["tri"], d["attr"], offsets, weights)
+    T = faces.shape[0]
+    return dict(name="msaa", host=host, setup=setup, step=step, units=64 * T, unit="Mtri-samples/s", scale=1e6,
+                metric="triangle samples rasterised, interpolated and resolved per second (64-sample MSAA)",
+                alg_bytes=64 * (16 * verts.shape[0] + 12 * T + 16 * H * W) + 20 * H * W, launches=None,
+                workload="64-sample software MSAA of a 400x64-strand wisp tube (403,200 triangles) into 512x256: "
+                         "all jitters in one fused raster + one resolve")
+
+
+WORKLOADS = {"msaa": wl_msaa, "resample": wl_resample, "tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
              "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
@@ -736,7 +791,10 @@ def run_workload(args):
     line = {"metric": wl["metric"], "value": value, "unit": wl["unit"], "n_gpus": 1, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": wl["workload"], "l2": "flushed between steps (256 MiB write)"},
+            "config": dict({"workload": wl["workload"], "l2": "flushed between steps (256 MiB write)"},
+                           **({"host_reference_algorithm_s": st["host_s"]} if isinstance(st, dict) and "host_s" in st
+                              else {}),
+                           **(st.get("config_extra", {}) if isinstance(st, dict) else {})),
             "e2e": {"value": e2e, "unit": wl["unit"], "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "algorithmic_bytes_per_step": wl["alg_bytes"], "traffic": None},

@@ -167,6 +167,14 @@ S2C_API s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* 
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream);
 
+/* new: resolve of a software-MSAA render (texture_utils.py:189-226): rast (S, H, W, 4) of S
+ * jittered rasterisations of one mesh; per pixel, in sample order, acc (H, W, C) += the
+ * interpolated attribute (as s2c_interpolate_triangle_attributes) * valid, count (H, W) +=
+ * valid, alpha (H, W) += weights[i] * valid, valid = rast.w > 0.  C <= 8. */
+S2C_API s2c_status s2c_msaa_resolve(int S, int H, int W, int C, const float* rast, int V, const float* attr, int T,
+                                    const int32_t* tri, const float* weights, float* acc, float* count,
+                                    float* alpha, s2c_stream stream);
+
 /* new: d(b0, b1)/d(x, y) in pixel units, rast_db (B, H, W, 4) = (db0/dx, db0/dy, db1/dx,
  * db1/dy), from the clip-space edge functions of the forward (rasterize.cu:144-156) for the
  * triangle id in rast (B, H, W, 4); 0 where rast is empty.  The reference has no such output. */

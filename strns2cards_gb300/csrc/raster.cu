@@ -401,6 +401,55 @@ __global__ void __launch_bounds__(256) interp_kernel(int64_t npix, const float4*
         image[p * C + d] = __fmaf_rn(b2, __ldg(a2 + d), __fmaf_rn(b1, __ldg(a1 + d), __fmul_rn(b0, __ldg(a0 + d))));
 }
 
+// Software MSAA resolve (the sample loop of the reference's texture render,
+// texture_utils.py:189-226, with interpolate_triangle_attributes folded in): per pixel and
+// sample i in order, rgb_i = the interpolated attribute of rast_i (0 where empty), a_i =
+// (rast_i.w > 0), acc += rgb_i * a_i, count += a_i, alpha += w_i * a_i -- the FP32 torch
+// operations of the reference's loop in the same order, so the sums are identical.
+constexpr int kMsaaMaxC = 8;
+
+__global__ void __launch_bounds__(256) msaa_resolve_kernel(int S, int64_t npix, int C, const float4* __restrict__ rast,
+                                                           const float* __restrict__ attr, int V,
+                                                           const int* __restrict__ tri, int T,
+                                                           const float* __restrict__ wts, float* __restrict__ acc,
+                                                           float* __restrict__ cnt, float* __restrict__ alpha) {
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += (int64_t)gridDim.x * blockDim.x) {
+        float a[kMsaaMaxC];
+#pragma unroll
+        for (int d = 0; d < kMsaaMaxC; ++d) a[d] = 0.f;
+        float n = 0.f, al = 0.f;
+        for (int i = 0; i < S; ++i) {
+            const float4 r = __ldcs(rast + (int64_t)i * npix + p);
+            const float av = r.w > 0.f ? 1.f : 0.f;
+            const int t = f2i(r.w) - 1;
+            bool ok = t >= 0 && t < T;
+            int v0 = 0, v1 = 0, v2 = 0;
+            if (ok) {
+                v0 = __ldg(tri + 3 * t);
+                v1 = __ldg(tri + 3 * t + 1);
+                v2 = __ldg(tri + 3 * t + 2);
+                ok = (unsigned)v0 < (unsigned)V && (unsigned)v1 < (unsigned)V && (unsigned)v2 < (unsigned)V;
+            }
+            const float b0 = r.x, b1 = r.y, b2 = __fsub_rn(__fsub_rn(1.f, b0), b1);
+#pragma unroll
+            for (int d = 0; d < kMsaaMaxC; ++d) {
+                if (d >= C) break;
+                float rgb = 0.f;
+                if (ok)
+                    rgb = __fmaf_rn(b2, __ldg(attr + (int64_t)C * v2 + d),
+                                    __fmaf_rn(b1, __ldg(attr + (int64_t)C * v1 + d),
+                                              __fmul_rn(b0, __ldg(attr + (int64_t)C * v0 + d))));
+                a[d] = __fadd_rn(a[d], __fmul_rn(rgb, av));
+            }
+            n = __fadd_rn(n, av);
+            al = __fadd_rn(al, __fmul_rn(__ldg(wts + i), av));
+        }
+        for (int d = 0; d < C; ++d) acc[p * C + d] = a[d];
+        cnt[p] = n;
+        alpha[p] = al;
+    }
+}
+
 // rasterize.cu:402-438: scatter-add of grad * b_i (float atomics, as the reference)
 __global__ void __launch_bounds__(256) interp_backward_kernel(int64_t npix, const float4* __restrict__ rast, int C,
                                                               const float* __restrict__ d_image,
@@ -790,5 +839,21 @@ static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* 
                                                                                            (float4*)rast);
         S2C_CHECK_LAUNCH("tri_resolve_kernel");
     }
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_msaa_resolve(int S, int H, int W, int C, const float* rast, int V, const float* attr, int T,
+                                       const int32_t* tri, const float* weights, float* acc, float* count,
+                                       float* alpha, s2c_stream stream) {
+    S2C_REQUIRE(S > 0 && H >= 0 && W >= 0 && C >= 0 && C <= kMsaaMaxC && V >= 0 && T >= 0,
+                "msaa_resolve: bad sizes (at most %d channels)", kMsaaMaxC);
+    const int64_t npix = (int64_t)H * W;
+    if (npix == 0) return S2C_OK;
+    S2C_REQUIRE(rast && weights && count && alpha && (C == 0 || (acc && attr)) && (T == 0 || tri),
+                "msaa_resolve: null pointer");
+    S2C_REQUIRE(((uintptr_t)rast & 15) == 0, "msaa_resolve: misaligned rast");
+    msaa_resolve_kernel<<<grid_for(npix, 256, (int64_t)num_sms() * 16), 256, 0, (cudaStream_t)stream>>>(
+        S, npix, C, (const float4*)rast, attr, V, tri, T, weights, acc, count, alpha);
+    S2C_CHECK_LAUNCH("msaa_resolve_kernel");
     return S2C_OK;
 }

@@ -240,3 +240,41 @@ def strand_scene(num_strands: int, num_verts: int, per_cluster: int, num_views: 
 # Named workloads (sizes of the published configurations)
 CONFIG_SMALL = dict(num_strands=1024, num_verts=32, per_cluster=16, H=256, W=256)
 CONFIG_FULL = dict(num_strands=50_000, num_verts=100, per_cluster=25, H=1024, W=1024)
+
+
+def tube_mesh(strands: np.ndarray, radius: float, n_circle: int = 8):
+    """Open tube around every strand (n_circle vertices per point), the topology of the
+    reference's ``strands_to_tube`` (curve_utils.py:310-374) with a simple frame: verts
+    (N*S*n, 3), faces (M, 3) int32, per-vertex unit tangents (N*S*n, 3)."""
+    N, S, _ = strands.shape
+    st = strands.astype(np.float64)
+    tan = np.zeros_like(st)
+    d = np.diff(st, axis=1)
+    tan[:, :-1] += d
+    tan[:, 1:] += d
+    tan /= np.maximum(np.linalg.norm(tan, axis=2, keepdims=True), 1e-12)
+    ref = np.where(np.abs(tan[..., 2:3]) < 0.9, np.array([0.0, 0.0, 1.0]), np.array([1.0, 0.0, 0.0]))
+    nrm = np.cross(tan, ref)
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=2, keepdims=True), 1e-12)
+    bin_ = np.cross(tan, nrm)
+    th = np.linspace(0, 2 * np.pi, n_circle, endpoint=False)
+    dirs = np.cos(th)[None, None, :, None] * nrm[:, :, None, :] + np.sin(th)[None, None, :, None] * bin_[:, :, None, :]
+    verts = (st[:, :, None, :] + radius * dirs).reshape(N * S * n_circle, 3)
+    idx = np.arange(S * n_circle).reshape(S, n_circle)
+    a, b = idx[:-1], np.roll(idx[:-1], -1, axis=1)
+    c, e = idx[1:], np.roll(idx[1:], -1, axis=1)
+    faces = np.stack([np.stack([a, c, e], -1), np.stack([a, e, b], -1)], 0).reshape(-1, 3)
+    faces = (faces[None] + (np.arange(N) * S * n_circle)[:, None, None]).reshape(-1, 3).astype(np.int32)
+    attr = np.repeat(tan[:, :, None, :], n_circle, axis=2).reshape(-1, 3)
+    return verts.astype(np.float32), faces, attr.astype(np.float32)
+
+
+def wisp_patch(num_strands: int, num_verts: int, n_circle: int = 8, seed: int = 0):
+    """A wisp of neighbouring strands as a tube mesh in NDC ([-0.9, 0.9] on x and y, z scaled
+    by 0.2 as the reference does to avoid depth clipping)."""
+    st = make_strands(num_strands, num_verts, seed=seed)
+    lo, hi = st.reshape(-1, 3).min(0), st.reshape(-1, 3).max(0)
+    scale = 1.8 / np.maximum(hi - lo, 1e-6)
+    ndc = (st - (lo + hi) / 2) * scale
+    ndc[..., 2] *= 0.2
+    return tube_mesh(ndc.astype(np.float32), radius=0.004, n_circle=n_circle)
