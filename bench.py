@@ -728,11 +728,108 @@ def wl_msaa():
                          "all jitters in one fused raster + one resolve")
 
 
+def _align_wisps_loop(strands, sizes, beta):
+    """The reference's align_wisps structure (curve_utils.py:104-165, 481-607) over the
+    drop-in ops, for the record: a Python loop over wisps with a host SVD of each wisp's
+    roots, and the Bishop frame as a loop over the points (torch ops on all strands)."""
+    import torch
+    import strns2cards_gb300 as s2c
+    dev = strands.device
+    lengths = (strands[:, 1:] - strands[:, :-1]).norm(dim=2).sum(1)
+    h_orig = s2c.smooth_strands(strands, beta)
+    Td = torch.tensor([0.0, 1.0, 0.0], device=dev)
+    Nd = torch.tensor([0.0, 0.0, -1.0], device=dev)
+    Bd = torch.tensor([-1.0, 0.0, 0.0], device=dev)
+    s_all, h_all, off = [], [], 0
+    for n in sizes.tolist():
+        sw, hw = strands[off:off + n].clone(), h_orig[off:off + n].clone()
+        c = sw[:, 0].mean(0, keepdim=True)
+        sw -= c
+        hw -= c
+        _, _, Vt = np.linalg.svd(sw[:, 0].cpu().numpy(), full_matrices=False)
+        ax = torch.from_numpy(Vt[:3] if Vt.shape == (3, 3) else np.eye(3, dtype=np.float32)).float().to(dev)
+        li = int(torch.argmax(lengths[off:off + n]).item())
+        g = sw[li]
+        view = (g[0] - g[1]) / (g[0] - g[1]).norm().clamp(min=1e-8)
+        down = (g[-1] - g[0]) / (g[-1] - g[0]).norm().clamp(min=1e-8)
+        sg = torch.sign(torch.dot(ax[2], view)).item()
+        nsrc = ax[2] * (1.0 if sg == 0 else sg)
+        tsrc = down - torch.dot(down, nsrc) * nsrc
+        tsrc = tsrc / tsrc.norm()
+        if not bool(torch.isfinite(tsrc).all()):
+            tsrc = ax[1]
+        Rg = torch.stack([Td, Nd, Bd], -1) @ torch.stack([tsrc, nsrc, torch.cross(tsrc, nsrc, dim=-1)], -1).T
+        s_all.append(sw.reshape(-1, 3) @ Rg.T)
+        h_all.append(hw.reshape(-1, 3) @ Rg.T)
+        off += n
+    S, V, _ = strands.shape
+    sr = torch.cat(s_all).reshape(S, V, 3)
+    hr = torch.cat(h_all).reshape(S, V, 3)
+    # Bishop frame: loop over the points
+    d = hr[:, 1:] - hr[:, :-1]
+    T = torch.zeros_like(hr)
+    T[:, :-1] += d
+    T[:, 1:] += d
+    T = T / T.norm(dim=-1, keepdim=True).clamp(min=1e-8)
+    N, B = torch.zeros_like(hr), torch.zeros_like(hr)
+    N[:, 0], B[:, 0] = s2c.tangent_frame(T[:, 0])
+    for i in range(1, V):
+        v1 = hr[:, i] - hr[:, i - 1]
+        c1 = (v1 ** 2).sum(-1, keepdim=True).clamp(min=1e-8)
+        nL = N[:, i - 1] - 2 * ((v1 * N[:, i - 1]).sum(-1, keepdim=True) / c1) * v1
+        tL = T[:, i - 1] - 2 * ((v1 * T[:, i - 1]).sum(-1, keepdim=True) / c1) * v1
+        v2 = T[:, i] - tL
+        c2 = (v2 ** 2).sum(-1, keepdim=True).clamp(min=1e-8)
+        n1 = nL - 2 * ((v2 * nL).sum(-1, keepdim=True) / c2) * v2
+        N[:, i] = n1 / n1.norm(dim=-1, keepdim=True).clamp(min=1e-8)
+        b1 = torch.cross(T[:, i], N[:, i], dim=-1)
+        B[:, i] = b1 / b1.norm(dim=-1, keepdim=True).clamp(min=1e-8)
+    Ra = s2c.minimal_rotation(T[:, 0], Td.expand(S, 3))
+    nd = (Ra @ N[:, 0, :, None])[..., 0]
+    bd = (Ra @ B[:, 0, :, None])[..., 0]
+    Rdst = torch.stack([Td.expand(S, V, 3), nd[:, None].expand(S, V, 3), bd[:, None].expand(S, V, 3)], -1)
+    R = Rdst @ torch.stack([T, N, B], -1).transpose(-1, -2)
+    arc = torch.cat([torch.zeros((S, 1), device=dev), torch.cumsum(d.norm(dim=2), 1)], 1)
+    canon = arc[..., None] * Td + sr[:, 0][:, None]
+    return s2c.skinning(sr, hr, canon, R.contiguous(), beta), h_orig
+
+
+def wl_align_wisps():
+    """align_wisps of 100,000 x 64 strands in 2,048 wisps (sizes 1..~500)."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    x, sizes = syn.make_wisps(100_000, 64, 2048, seed=0)
+    host = {"x": x}
+    sz = torch.from_numpy(sizes)
+
+    def setup(d):
+        _align_wisps_loop(d["x"], sz, 0.05)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _align_wisps_loop(d["x"], sz, 0.05)
+        b.record()
+        torch.cuda.synchronize()
+        return {"config_extra": {"per_wisp_loop_ms": a.elapsed_time(b)}}
+
+    def step(d, st):
+        return s2c.align_wisps_packed(d["x"], sz, 0.05)
+    n = x.shape[0] * x.shape[1]
+    # smooth (read 12, write 12) + wisp frames (read roots + lengths: 12) + rotate (read 24, write 24)
+    # + frames (read 12 + roots, write R 36 + canon 12) + skinning (read 12*3 + 36, write 12) per point
+    return dict(name="align_wisps", host=host, setup=setup, step=step, units=n, unit="Mpts/s", scale=1e6,
+                metric="strand points aligned per second (align_wisps)",
+                alg_bytes=(24 + 12 + 48 + 60 + 84) * n, launches=None,
+                workload="align_wisps of 100,000 x 64 strands in 2,048 wisps, beta 0.05: smoothing, per-wisp "
+                         "frames, rotation, Bishop frames + canonical handles, skinning")
+
+
 WORKLOADS = {"msaa": wl_msaa, "resample": wl_resample, "tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
              "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
-             "laplacian": wl_laplacian}
+             "laplacian": wl_laplacian, "align_wisps": wl_align_wisps}
 
 
 def run_workload(args):

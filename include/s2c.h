@@ -336,6 +336,42 @@ S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float*
                                 const float* R, float* skinned_strands, float beta,
                                 s2c_stream stream);
 
+/* replaces: compute_bishop_frame, compute_alignment_rotation, compute_aligned_strands
+ * (curve_utils.py:104-165, 273-308, 243-271), one thread per strand, FP32.
+ * strands (N, V, 3).  Every output may be NULL:
+ *   T, Nrm, Bin (N, V, 3): the double-reflection rotation-minimising frame, started from
+ *     tangent_frame of the root tangent (curve_utils.py:76-102);
+ *   R (N, V, 3, 3) row-major: [t_dst n_dst b_dst][T N B]^T, n_dst, b_dst the root frame
+ *     turned by the minimal rotation of the root tangent onto t_dst;
+ *   canon (N, V, 3): arclength * t_dst + root, the roots taken from `roots` (one per strand,
+ *     roots_stride floats apart: 3 for an (N, 3) array, 3V for the first points of an
+ *     (N, V, 3) array) or, when roots is NULL, from the strands themselves.
+ * t_dst: 3 floats in HOST memory (needed for R and canon). */
+S2C_API s2c_status s2c_strand_frames(int N, int V, const float* strands, const float* t_dst, float* T,
+                                     float* Nrm, float* Bin, float* R, const float* roots,
+                                     int64_t roots_stride, float* canon, s2c_stream stream);
+
+/* replaces: the per-wisp loop of align_wisps (curve_utils.py:521-568): one CTA per wisp.
+ * Wisp w holds strands offsets[w] .. offsets[w+1]-1 of strands (num_strands, V, 3), V >= 2.
+ * centre[w] = mean root; longest[w] = the strand of greatest polyline length (first on
+ * ties); the least-variance axis of the centred roots (FP64 second moment and a Jacobi
+ * eigen-solve, in place of the host SVD; identity axes below 3 strands) and the longest
+ * strand's view and down directions give the source frame; R_global[w] (3x3 row-major) =
+ * [t_dst n_dst b_dst][T_src N_src B_src]^T.  An empty or out-of-range wisp gets the
+ * identity, centre 0 and longest -1.  t_dst, n_dst, b_dst: 3 floats each in HOST memory. */
+S2C_API s2c_status s2c_wisp_frames(int num_wisps, const int32_t* offsets, int64_t num_strands, int V,
+                                   const float* strands, const float* t_dst, const float* n_dst,
+                                   const float* b_dst, float* R_global, float* centre, int32_t* longest,
+                                   s2c_stream stream);
+
+/* new: a_out = R_global[w] (a - centre[w]) and b_out likewise for every point of every strand,
+ * w the wisp whose range offsets[w] .. offsets[w+1]-1 holds the strand (offsets as for
+ * s2c_wisp_frames, non-decreasing); a strand of no wisp is copied unchanged
+ * (curve_utils.py:567-568 rotate the strands and the handle strands of each wisp). */
+S2C_API s2c_status s2c_wisp_rotate(int num_wisps, const int32_t* offsets, int64_t num_strands, int V,
+                                   const float* R_global, const float* centre, const float* a,
+                                   const float* b, float* a_out, float* b_out, s2c_stream stream);
+
 /* replaces: load_strands (pystrns2cards.cpp:788-816; hair_loader.cpp:15-259).  Host.
  * Reads a .bin, .data (USC) or .hair (CY-HAIR / ZJU) file; *handle receives the strands
  * with at least two points (counts in *num_strands, total points in *num_points), to be

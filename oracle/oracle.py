@@ -437,3 +437,187 @@ def barycentric_derivatives(rast, pos, tri):
         out[b, y, x, 2 * i] = np.where(ok, (dAx[:, i] - bb[:, i] * dAx.sum(1)) / np.where(ok, S, 1.0) * (2.0 / W), 0.0)
         out[b, y, x, 2 * i + 1] = np.where(ok, (dAy[:, i] - bb[:, i] * dAy.sum(1)) / np.where(ok, S, 1.0) * (2.0 / H), 0.0)
     return out
+
+
+# ---- strand frames and wisp alignment (curve_utils.py:9-165, 243-308, 481-607), FP64 numpy
+def tangent_frame(t):
+    """curve_utils.py:76-102: branch-free orthonormal (normal, binormal) around t."""
+    t = np.asarray(t, np.float64)
+    t = t / np.maximum(np.linalg.norm(t, axis=-1, keepdims=True), 1e-8)
+    x, y, z = t[..., 0], t[..., 1], t[..., 2]
+    sign = np.where(z > 0, 1.0, np.where(z < 0, -1.0, 1.0))
+    a = -1.0 / (sign + z)
+    b = x * y * a
+    n = np.stack([1.0 + sign * x * x * a, sign * b, -sign * x], -1)
+    bn = np.stack([b, sign + y * y * a, -y], -1)
+    return n, bn
+
+
+def minimal_rotation(src, dst):
+    """curve_utils.py:9-74: Rodrigues rotation taking src onto dst; identity when parallel
+    (cos > 1 - 1e-6), diag(-1, -1, 1) when antiparallel (cos < -1 + 1e-6)."""
+    s = np.asarray(src, np.float64)
+    d = np.broadcast_to(np.asarray(dst, np.float64), s.shape)
+    s = s / np.maximum(np.linalg.norm(s, axis=-1, keepdims=True), 1e-8)
+    d = d / np.maximum(np.linalg.norm(d, axis=-1, keepdims=True), 1e-8)
+    ax = np.cross(s, d)
+    sn = np.linalg.norm(ax, axis=-1)
+    cs = np.clip((s * d).sum(-1), -1.0, 1.0)
+    ax = ax / np.maximum(sn, 1e-8)[..., None]
+    K = np.zeros(s.shape[:-1] + (3, 3))
+    K[..., 0, 1], K[..., 0, 2] = -ax[..., 2], ax[..., 1]
+    K[..., 1, 0], K[..., 1, 2] = ax[..., 2], -ax[..., 0]
+    K[..., 2, 0], K[..., 2, 1] = -ax[..., 1], ax[..., 0]
+    R = np.eye(3) + sn[..., None, None] * K + (1.0 - cs)[..., None, None] * (K @ K)
+    R = np.where((cs > 1 - 1e-6)[..., None, None], np.eye(3), R)
+    return np.where((cs < -1 + 1e-6)[..., None, None], np.diag([-1.0, -1.0, 1.0]), R)
+
+
+def bishop_frame(strands):
+    """curve_utils.py:104-165: double-reflection rotation-minimising frame (T, N, B)."""
+    p = np.asarray(strands, np.float64)
+    d = p[:, 1:] - p[:, :-1]
+    T = np.zeros_like(p)
+    T[:, :-1] += d
+    T[:, 1:] += d
+    T = T / np.maximum(np.linalg.norm(T, axis=-1, keepdims=True), 1e-8)
+    N = np.zeros_like(p)
+    B = np.zeros_like(p)
+    N[:, 0], B[:, 0] = tangent_frame(T[:, 0])
+
+    def dot(a, b):
+        return (a * b).sum(-1, keepdims=True)
+
+    for i in range(1, p.shape[1]):
+        v1 = p[:, i] - p[:, i - 1]
+        c1 = np.maximum(dot(v1, v1), 1e-8)
+        nL = N[:, i - 1] - 2 * (dot(v1, N[:, i - 1]) / c1) * v1
+        tL = T[:, i - 1] - 2 * (dot(v1, T[:, i - 1]) / c1) * v1
+        v2 = T[:, i] - tL
+        c2 = np.maximum(dot(v2, v2), 1e-8)
+        n1 = nL - 2 * (dot(v2, nL) / c2) * v2
+        n1 = n1 / np.maximum(np.linalg.norm(n1, axis=-1, keepdims=True), 1e-8)
+        b1 = np.cross(T[:, i], n1)
+        B[:, i] = b1 / np.maximum(np.linalg.norm(b1, axis=-1, keepdims=True), 1e-8)
+        N[:, i] = n1
+    return T, N, B
+
+
+def alignment_rotation(strands, t_dst):
+    """curve_utils.py:273-308: R = [t_dst n_dst b_dst][T N B]^T per point, (n_dst, b_dst) the
+    root frame turned by the minimal rotation of the root tangent onto t_dst."""
+    T, N, B = bishop_frame(strands)
+    td = np.broadcast_to(np.asarray(t_dst, np.float64).reshape(3), T.shape)
+    Ra = minimal_rotation(T[:, 0], td[:, 0])
+    nd = np.einsum("sij,sj->si", Ra, N[:, 0])
+    bd = np.einsum("sij,sj->si", Ra, B[:, 0])
+    Rdst = np.stack([td, np.broadcast_to(nd[:, None], T.shape), np.broadcast_to(bd[:, None], T.shape)], -1)
+    Rsrc = np.stack([T, N, B], -1)
+    return Rdst @ np.swapaxes(Rsrc, -1, -2)
+
+
+def aligned_strands(strands, roots, t_dst):
+    """curve_utils.py:243-271: arclength * t_dst + root."""
+    p = np.asarray(strands, np.float64)
+    arc = np.concatenate([np.zeros((p.shape[0], 1)), np.cumsum(np.linalg.norm(p[:, 1:] - p[:, :-1], axis=-1), 1)], 1)
+    return arc[..., None] * np.asarray(t_dst, np.float64).reshape(1, 1, 3) + np.asarray(roots, np.float64)[:, None]
+
+
+WISP_T_DST = np.array([0.0, 1.0, 0.0])
+WISP_N_DST = np.array([0.0, 0.0, -1.0])
+WISP_B_DST = np.array([-1.0, 0.0, 0.0])
+
+
+def wisp_frame(strands):
+    """The loop body of align_wisps (curve_utils.py:521-568) for one wisp's float32 strands:
+    (R_global, root centre, index of the longest strand), with the same numpy SVD call."""
+    p = np.asarray(strands, np.float32).astype(np.float64)
+    lengths = np.linalg.norm(p[:, 1:] - p[:, :-1], axis=-1).sum(1)
+    centre = p[:, 0].mean(0)
+    q = p - centre
+    roots = q[:, 0]
+    try:
+        _, _, Vt = np.linalg.svd(roots, full_matrices=False)
+        axes = Vt[:3] if Vt.shape == (3, 3) and np.all(np.isfinite(Vt[:3])) else np.eye(3)
+    except np.linalg.LinAlgError:
+        axes = np.eye(3)
+    least, second = axes[2], axes[1]
+    li = int(np.argmax(lengths))
+    g = q[li]
+    view = g[0] - g[1]
+    view = view / max(np.linalg.norm(view), 1e-8)
+    down = g[-1] - g[0]
+    down = down / max(np.linalg.norm(down), 1e-8)
+    sg = np.sign(least @ view)
+    nsrc = least * (1.0 if sg == 0 else sg)
+    tsrc = down - (down @ nsrc) * nsrc
+    with np.errstate(invalid="ignore", divide="ignore"):
+        tsrc = tsrc / np.linalg.norm(tsrc)
+    if not np.all(np.isfinite(tsrc)):
+        tsrc = second
+    bsrc = np.cross(tsrc, nsrc)
+    Rsrc = np.stack([tsrc, nsrc, bsrc], -1)
+    Rdst = np.stack([WISP_T_DST, WISP_N_DST, WISP_B_DST], -1)
+    return Rdst @ Rsrc.T, centre, li
+
+
+def align_wisps(wisps, beta):
+    """curve_utils.py:481-607 with the stages' float32 hand-offs: (aligned strands, smoothed
+    strands before alignment, global index of each wisp's longest strand)."""
+    arrs = [np.asarray(w, np.float32) for w in wisps]
+    strands = np.concatenate(arrs, 0)
+    arc = np.concatenate([np.zeros((strands.shape[0], 1), np.float32),
+                          np.cumsum(np.linalg.norm(strands[:, 1:] - strands[:, :-1], axis=-1), 1)], 1)
+    handles = smooth_strands(strands, arc, beta).astype(np.float32)
+    s_rot, h_rot, longest = [], [], []
+    off = 0
+    for w in arrs:
+        R, c, li = wisp_frame(w)
+        s_rot.append((w.astype(np.float64) - c) @ R.T)
+        h_rot.append((handles[off:off + w.shape[0]].astype(np.float64) - c) @ R.T)
+        longest.append(off + li)
+        off += w.shape[0]
+    s_rot = np.concatenate(s_rot).astype(np.float32)
+    h_rot = np.concatenate(h_rot).astype(np.float32)
+    canon = aligned_strands(h_rot, s_rot[:, 0], WISP_T_DST).astype(np.float32)
+    Rl = alignment_rotation(h_rot, WISP_T_DST).astype(np.float32)
+    arc_s = np.concatenate([np.zeros((s_rot.shape[0], 1), np.float32),
+                            np.cumsum(np.linalg.norm(s_rot[:, 1:] - s_rot[:, :-1], axis=-1), 1)], 1)
+    out = skinning(s_rot, arc_s, h_rot, canon, Rl, beta)
+    return out, handles, np.asarray(longest, np.int64)
+
+
+def align_wisp(strands, beta):
+    """curve_utils.py:376-479 (one wisp): (aligned strands, smoothed strands in the aligned
+    frame, index of the longest strand), FP64 between float32 hand-offs."""
+    p = np.asarray(strands, np.float32).astype(np.float64)
+    p = p - p[:, 0].mean(0)
+    _, _, Vt = np.linalg.svd(p[:, 0], full_matrices=False)
+    pa = Vt[0] if np.all(np.isfinite(Vt[0])) else np.array([1.0, 0.0, 0.0])
+    li = int(np.argmax(np.linalg.norm(p[:, 1:] - p[:, :-1], axis=-1).sum(1)))
+    p32 = p.astype(np.float32)
+    arc = np.concatenate([np.zeros((p.shape[0], 1), np.float32),
+                          np.cumsum(np.linalg.norm(p32[:, 1:] - p32[:, :-1], axis=-1), 1)], 1)
+    h = smooth_strands(p32, arc, beta)
+    g = h[li]
+    t0, t1 = g[1] - g[0], g[2] - g[1]
+    t0 = t0 - (t0 @ pa) * pa
+    t1 = t1 - (t1 @ pa) * pa
+    t0, t1 = t0 / np.linalg.norm(t0), t1 / np.linalg.norm(t1)
+    b0 = np.cross(t0, t1)
+    b0 = b0 / np.linalg.norm(b0)
+    n0 = np.cross(b0, t0)
+    n0 = n0 / np.linalg.norm(n0)
+    if not (np.all(np.isfinite(n0)) and np.all(np.isfinite(b0))):
+        n0, b0 = tangent_frame(t0)
+    Rsrc = np.stack([t0, n0, b0], -1)
+    Rdst = np.stack([[0.0, -1.0, 0.0], [0.0, 0.0, -1.0], [1.0, 0.0, 0.0]], -1)
+    Rg = Rdst @ Rsrc.T
+    s_rot = (p @ Rg.T).astype(np.float32)
+    h_rot = (h @ Rg.T).astype(np.float32)
+    td = np.array([0.0, -1.0, 0.0])
+    canon = aligned_strands(h_rot, s_rot[:, 0], td).astype(np.float32)
+    Rl = alignment_rotation(h_rot, td).astype(np.float32)
+    arc_s = np.concatenate([np.zeros((p.shape[0], 1), np.float32),
+                            np.cumsum(np.linalg.norm(s_rot[:, 1:] - s_rot[:, :-1], axis=-1), 1)], 1)
+    return skinning(s_rot, arc_s, h_rot, canon, Rl, beta), h_rot, li

@@ -6,7 +6,9 @@ so that ``import strns2cards_gb300 as s2c`` replaces ``import pystrns2cards as s
 from .antialias import (antialiased_cluster_bitset_grad, antialiased_cluster_bitset_loss,  # noqa: F401
                         mark_discontinuity_edges)
 from .deform import CardLaplacian, LBSBinding, card_laplacian_smooth, lbs, vertex_adjacency  # noqa: F401
-from .curve_utils import compute_arclength, skinning, smooth_strands  # noqa: F401
+from .curve_utils import (align_wisp, align_wisps, align_wisps_packed, compute_aligned_strands,  # noqa: F401
+                          compute_alignment_rotation, compute_arclength, compute_bishop_frame, minimal_rotation,
+                          skinning, smooth_strands, strands_to_tube, tangent_frame)
 from .bitset_utils import accumulate_bitset_rgb, cluster_iou, popcount_bitset, xor_error  # noqa: F401
 from .dda import (DDAInterpolateAttributes, dda_cluster_bitset, dda_compute_fragments,  # noqa: F401
                   dda_interpolate_attributes)

@@ -551,6 +551,79 @@ def skinning(strands, arclength, handle_strands, canonical_handles, R, skinned_s
          ptr(skinned_strands), float(beta), _stream(strands))
 
 
+# ---- strand frames and wisp alignment (curve_utils.py:104-165, 243-308, 481-607) ----------
+def _vec3(v):
+    v = [float(x) for x in (v.tolist() if hasattr(v, "tolist") else v)]
+    if len(v) != 3:
+        raise RuntimeError("expected a 3-vector")
+    return (ctypes.c_float * 3)(*v)
+
+
+def strand_frames(strands, t_dst=None, T=None, N=None, B=None, R=None, roots=None, canon=None) -> None:
+    """Bishop frames (T, N, B), alignment rotations R and canonical handles ``canon`` of
+    strands (S, V, 3) in one launch; every output optional.  ``roots`` is an (S, 3) tensor or
+    a strided view of one point per strand (e.g. ``x[:, 0]`` of an (S, V, 3) tensor)."""
+    _arr(strands, _f32, 3, 3, "strands")
+    S, V, _ = strands.shape
+    for t, nm in ((T, "T"), (N, "N"), (B, "B"), (canon, "canon")):
+        if t is not None:
+            _arr(t, _f32, 3, 3, nm)
+            if tuple(t.shape) != (S, V, 3):
+                raise RuntimeError(f"strand_frames: {nm} must match (num_strands, num_points, 3).")
+    if R is not None:
+        _arr(R, _f32, 4, 3, "R")
+        if tuple(R.shape) != (S, V, 3, 3):
+            raise RuntimeError("strand_frames: R must match (num_strands, num_points, 3, 3).")
+    stride = 3
+    if roots is not None:
+        if not isinstance(roots, torch.Tensor) or roots.dtype != _f32 or roots.ndim != 2 or tuple(roots.shape) != (S, 3):
+            raise RuntimeError("strand_frames: roots must be float32 (num_strands, 3).")
+        if roots.stride(1) != 1 or (S > 1 and roots.stride(0) < 3):
+            raise RuntimeError("strand_frames: roots must be rows of 3 contiguous floats.")
+        stride = roots.stride(0) if S > 1 else 3
+    if (R is not None or canon is not None) and t_dst is None:
+        raise RuntimeError("strand_frames: R and canon need t_dst.")
+    _cuda(strands, T, N, B, R, roots, canon, msg="strand_frames: All input tensors must be CUDA.")
+    call("s2c_strand_frames", S, V, ptr(strands), _vec3(t_dst) if t_dst is not None else None, ptr(T), ptr(N), ptr(B),
+         ptr(R), ptr(roots), stride, ptr(canon), _stream(strands))
+
+
+def wisp_frames(offsets, strands, t_dst, n_dst, b_dst, R_global, centre, longest) -> None:
+    """Per-wisp centre, longest strand and global rotation (``align_wisps``'s loop body)."""
+    _arr(offsets, _i32, 1, name="offsets")
+    _arr(strands, _f32, 3, 3, "strands")
+    _arr(R_global, _f32, 3, 3, "R_global")
+    _arr(centre, _f32, 2, 3, "centre")
+    _arr(longest, _i32, 1, name="longest")
+    _cuda(offsets, strands, R_global, centre, longest, msg="wisp_frames: All input tensors must be CUDA.")
+    K = offsets.shape[0] - 1
+    if K < 0 or R_global.shape[0] != K or centre.shape[0] != K or longest.shape[0] != K:
+        raise RuntimeError("wisp_frames: outputs must hold one row per wisp.")
+    S, V, _ = strands.shape
+    if V < 2:
+        raise RuntimeError("wisp_frames: strands need at least 2 points.")
+    call("s2c_wisp_frames", K, ptr(offsets), S, V, ptr(strands), _vec3(t_dst), _vec3(n_dst), _vec3(b_dst),
+         ptr(R_global), ptr(centre), ptr(longest), _stream(strands))
+
+
+def wisp_rotate(offsets, R_global, centre, a, b, a_out, b_out) -> None:
+    """a_out = R (a - c), b_out = R (b - c) with the frame of each strand's wisp (wisp w = the
+    strands offsets[w] .. offsets[w+1]-1)."""
+    for t, nm in ((a, "a"), (b, "b"), (a_out, "a_out"), (b_out, "b_out")):
+        _arr(t, _f32, 3, 3, nm)
+    _arr(offsets, _i32, 1, name="offsets")
+    _arr(R_global, _f32, 3, 3, "R_global")
+    _arr(centre, _f32, 2, 3, "centre")
+    _cuda(offsets, R_global, centre, a, b, a_out, b_out, msg="wisp_rotate: All input tensors must be CUDA.")
+    S, V, _ = a.shape
+    K = offsets.shape[0] - 1
+    if any(tuple(t.shape) != (S, V, 3) for t in (b, a_out, b_out)) or K < 0 or R_global.shape[0] != K \
+            or centre.shape[0] != K:
+        raise RuntimeError("wisp_rotate: shapes do not match.")
+    call("s2c_wisp_rotate", K, ptr(offsets), S, V, ptr(R_global), ptr(centre), ptr(a), ptr(b), ptr(a_out), ptr(b_out),
+         _stream(a))
+
+
 # ---- strand ingest (pystrns2cards.cpp:788-839) -----------------------------------------
 def load_strands(filepath):
     """Host: (num_samples int32 (N, 1), points float32 (P, 3)) of a .bin/.data/.hair file."""

@@ -75,6 +75,9 @@ SIGNATURES = {
     "s2c_compute_arclength": ([c_i, c_i, vp, vp, vp], c_i),
     "s2c_smooth_strands": ([c_i, c_i, vp, vp, vp, c_f, vp], c_i),
     "s2c_skinning": ([c_i, c_i, vp, vp, vp, vp, vp, vp, c_f, vp], c_i),
+    "s2c_strand_frames": ([c_i, c_i, vp, vp, vp, vp, vp, vp, vp, c_i64, vp, vp], c_i),
+    "s2c_wisp_frames": ([c_i, vp, c_i64, c_i, vp, vp, vp, vp, vp, vp, vp, vp], c_i),
+    "s2c_wisp_rotate": ([c_i, vp, c_i64, c_i, vp, vp, vp, vp, vp, vp, vp], c_i),
     "s2c_build_edges_from_triangles": ([c_i, vp, vp, vp, i64p], c_i),
     "s2c_load_strands": ([ctypes.c_char_p, ctypes.POINTER(vp), i64p, i64p], c_i),
     "s2c_strands_take": ([vp, vp, vp], c_i),

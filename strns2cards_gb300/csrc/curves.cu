@@ -8,6 +8,8 @@
 // and gives every point its own thread, so the O(V^2) pair loop reads broadcast shared
 // memory.  Per point i the sum runs over j = 0..V-1 in order and skips pairs with
 // |a_i - a_j| > 3 beta exactly as the reference does; weights exp(-d^2 / beta^2) use expf.
+// With the arclength computed in the kernel the loop visits only the run of j inside the
+// cutoff (same terms, same order).
 #include <algorithm>
 
 #include "common.cuh"
@@ -51,6 +53,14 @@ __device__ __forceinline__ void warp_arclength(const float* x, int V, float* arc
         for (int o = 1; o < 32; o <<= 1) {
             const float t = __shfl_up_sync(0xffffffffu, d, o);
             if (lane >= o) d = __fadd_rn(d, t);
+        }
+        // the scan's sums take different rounding paths per lane; a running maximum (exact,
+        // and a NaN stays NaN) keeps the arclength non-decreasing, which the pair windows of
+        // curve_kernel rely on
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float t = __shfl_up_sync(0xffffffffu, d, o);
+            if (lane >= o && t > d) d = t;
         }
         if (i < V) arc[i] = __fadd_rn(carry, d);
         carry = __fadd_rn(carry, __shfl_sync(0xffffffffu, d, 31));
@@ -109,7 +119,18 @@ __global__ void __launch_bounds__(kCurveThreads) curve_kernel(CurveArgs a) {
             float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, sw = 0.f;
             float xi0 = 0.f, xi1 = 0.f, xi2 = 0.f;
             if (kSkin) { xi0 = X[3 * p]; xi1 = X[3 * p + 1]; xi2 = X[3 * p + 2]; }
-            for (int j = 0; j < V; ++j) {
+            // With the arclength computed here (non-decreasing along the strand) the points
+            // within the cutoff of point i form one run around i: walk out to its ends and sum
+            // over it in ascending order, the same terms in the same order as the full loop.
+            // A caller's arclength, or a non-finite one, takes the full loop.
+            int jlo = 0, jhi = V - 1;
+            if (!a.arc && isfinite(si) && isfinite(sarc[b + V - 1])) {
+                jlo = i;
+                while (jlo > 0 && !(fabsf(__fsub_rn(si, sarc[b + jlo - 1])) > cutoff)) --jlo;
+                jhi = i;
+                while (jhi < V - 1 && !(fabsf(__fsub_rn(si, sarc[b + jhi + 1])) > cutoff)) ++jhi;
+            }
+            for (int j = jlo; j <= jhi; ++j) {
                 const float dist = fabsf(__fsub_rn(si, sarc[b + j]));
                 if (dist > cutoff) continue;
                 const float w = expf(__fmul_rn(-__fmul_rn(dist, dist), inv_beta2));

@@ -278,3 +278,18 @@ def wisp_patch(num_strands: int, num_verts: int, n_circle: int = 8, seed: int = 
     ndc = (st - (lo + hi) / 2) * scale
     ndc[..., 2] *= 0.2
     return tube_mesh(ndc.astype(np.float32), radius=0.004, n_circle=n_circle)
+
+
+def make_wisps(num_strands: int, num_verts: int, num_wisps: int, seed: int = 0):
+    """Strands grouped into wisps: the generator's strands (Morton order, so neighbours share
+    a wisp) with lengths scaled per strand by a factor in [0.6, 1.0] about the root, cut into
+    ``num_wisps`` contiguous groups of random positive sizes.  Returns (strands (N, V, 3)
+    float32, sizes (num_wisps,) int64)."""
+    rng = np.random.default_rng(seed + 101)
+    st = make_strands(num_strands, num_verts, seed=seed).astype(np.float64)
+    f = rng.uniform(0.6, 1.0, size=(num_strands, 1, 1))
+    st = st[:, :1] + f * (st - st[:, :1])
+    K = max(1, min(num_wisps, num_strands))
+    cuts = np.sort(rng.choice(np.arange(1, num_strands), size=K - 1, replace=False)) if K > 1 else np.array([], int)
+    sizes = np.diff(np.concatenate([[0], cuts, [num_strands]])).astype(np.int64)
+    return _quantise(st), sizes
