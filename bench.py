@@ -816,20 +816,49 @@ def wl_align_wisps():
     def step(d, st):
         return s2c.align_wisps_packed(d["x"], sz, 0.05)
     n = x.shape[0] * x.shape[1]
-    # smooth (read 12, write 12) + wisp frames (read roots + lengths: 12) + rotate (read 24, write 24)
-    # + frames (read 12 + roots, write R 36 + canon 12) + skinning (read 12*3 + 36, write 12) per point
+    # wisp frames (read every point for the lengths: 12) + fused smoothing / rotation / frames /
+    # skinning (read 12, write handles 12 and aligned strands 12) per point
     return dict(name="align_wisps", host=host, setup=setup, step=step, units=n, unit="Mpts/s", scale=1e6,
                 metric="strand points aligned per second (align_wisps)",
-                alg_bytes=(24 + 12 + 48 + 60 + 84) * n, launches=None,
-                workload="align_wisps of 100,000 x 64 strands in 2,048 wisps, beta 0.05: smoothing, per-wisp "
-                         "frames, rotation, Bishop frames + canonical handles, skinning")
+                alg_bytes=(12 + 12 + 24) * n, launches=2,
+                workload="align_wisps of 100,000 x 64 strands in 2,048 wisps, beta 0.05: per-wisp frames, then "
+                         "smoothing, rotation, Bishop frames + canonical handles and skinning fused")
+
+
+def wl_build_edges():
+    """Edges of the card mesh of 2,048 cards (16 x 4 quads: 174,080 vertices, 262,144
+    triangles) on the device; the host builder timed for the record."""
+    import time
+    import torch
+    import strns2cards_gb300 as s2c
+    _, _, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
+    tri = np.ascontiguousarray(cards.tri, dtype=np.int32)
+    nv = int(cards.verts.shape[0])
+    host = {"tri": tri}
+
+    def setup(d):
+        s2c.build_edges_from_triangles(tri)
+        t0 = time.perf_counter()
+        s2c.build_edges_from_triangles(tri)
+        return {"config_extra": {"host_builder_ms": 1e3 * (time.perf_counter() - t0)}}
+
+    def step(d, st):
+        return s2c.build_edges_from_triangles_device(d["tri"], nv)
+    T = tri.shape[0]
+    # triangles read (12 B per triangle, twice), per half-edge: bucket/sorted/flag/eid writes and
+    # reads (4 B each, about 8 passes), edges + edge2tri written (16 B per edge, E ~ 1.5 T)
+    return dict(name="build_edges", host=host, setup=setup, step=step, units=T, unit="Mtri/s", scale=1e6, dtype="i32",
+                metric="card-mesh triangles turned into edges per second (device edge builder)",
+                alg_bytes=24 * T + 3 * T * 32 + 16 * 3 * T // 2, launches=None,
+                workload="unique edges + edge->triangle map of 2,048 cards (16x4 quads, 262,144 triangles) "
+                         "on the device, in the host builder's order")
 
 
 WORKLOADS = {"msaa": wl_msaa, "resample": wl_resample, "tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
              "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
-             "laplacian": wl_laplacian, "align_wisps": wl_align_wisps}
+             "laplacian": wl_laplacian, "align_wisps": wl_align_wisps, "build_edges": wl_build_edges}
 
 
 def run_workload(args):
@@ -887,7 +916,7 @@ def run_workload(args):
     achieved = wl["alg_bytes"] / (t / args.steps) / 1e9
     line = {"metric": wl["metric"], "value": value, "unit": wl["unit"], "n_gpus": 1, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": wl.get("dtype", "f32"), "data": "synthetic",
             "config": dict({"workload": wl["workload"], "l2": "flushed between steps (256 MiB write)"},
                            **({"host_reference_algorithm_s": st["host_s"]} if isinstance(st, dict) and "host_s" in st
                               else {}),

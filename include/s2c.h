@@ -372,6 +372,19 @@ S2C_API s2c_status s2c_wisp_rotate(int num_wisps, const int32_t* offsets, int64_
                                    const float* R_global, const float* centre, const float* a,
                                    const float* b, float* a_out, float* b_out, s2c_stream stream);
 
+/* replaces: the rest of align_wisps after its per-wisp loop (curve_utils.py:487-606), fused:
+ * per strand, handles = smooth_strands(strands, beta) (written out: align_wisps returns it),
+ * then the strand and its handle turned into its wisp's frame as s2c_wisp_rotate does, the
+ * handle's frames, alignment rotations and canonical handles (roots: the turned strand's
+ * first point) as s2c_strand_frames does, and the turned strand skinned to them as
+ * s2c_skinning does -- the same results bit for bit, with the intermediates kept in shared
+ * memory.  Needs 2 <= V <= s2c_align_strands_max_points(); t_dst: 3 floats in HOST memory. */
+S2C_API int s2c_align_strands_max_points(void);
+S2C_API s2c_status s2c_align_strands(int64_t num_strands, int V, const float* strands, int num_wisps,
+                                     const int32_t* offsets, const float* R_global, const float* centre,
+                                     const float* t_dst, float beta, float* handles, float* aligned,
+                                     s2c_stream stream);
+
 /* replaces: load_strands (pystrns2cards.cpp:788-816; hair_loader.cpp:15-259).  Host.
  * Reads a .bin, .data (USC) or .hair (CY-HAIR / ZJU) file; *handle receives the strands
  * with at least two points (counts in *num_strands, total points in *num_points), to be
@@ -406,6 +419,16 @@ S2C_API s2c_status s2c_resample_strands_by_arclength(int num_strands, const int3
  * edges and edge2tri hold 3*T rows; *num_edges receives the count. */
 S2C_API s2c_status s2c_build_edges_from_triangles(int T, const int32_t* tri, int32_t* edges,
                                                   int32_t* edge2tri, int64_t* num_edges);
+
+/* new: the same on the device, with the same edges in the same order and the same
+ * edge2tri (deterministic: buckets per min vertex, each ordered by (max vertex, half-edge)).
+ * tri (T, 3) device; edges and edge2tri hold 3*T rows; *num_edges (device int64) receives
+ * the edge count and *num_bad (device int32) the half-edges left out for a vertex outside
+ * [0, num_verts).  No host synchronisation. */
+S2C_API size_t s2c_build_edges_device_workspace_size(int T, int num_verts);
+S2C_API s2c_status s2c_build_edges_device(int T, const int32_t* tri, int num_verts, int32_t* edges,
+                                          int32_t* edge2tri, int64_t* num_edges, int32_t* num_bad,
+                                          void* workspace, size_t workspace_bytes, s2c_stream stream);
 
 /* new: host.  CSR vertex adjacency of an undirected edge list (the uniform Laplacian's
  * A of optimizer.py:70-99): neighbours of v in edge order, offsets (num_verts + 1),

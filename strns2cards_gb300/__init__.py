@@ -12,7 +12,7 @@ from .curve_utils import (align_wisp, align_wisps, align_wisps_packed, compute_a
 from .bitset_utils import accumulate_bitset_rgb, cluster_iou, popcount_bitset, xor_error  # noqa: F401
 from .dda import (DDAInterpolateAttributes, dda_cluster_bitset, dda_compute_fragments,  # noqa: F401
                   dda_interpolate_attributes)
-from .mesh import build_edges_from_triangles  # noqa: F401
+from .mesh import build_edges_from_triangles, build_edges_from_triangles_device  # noqa: F401
 from .texture import msaa_pattern, msaa_render, msaa_render_loop, resolve_patch  # noqa: F401
 from .strands import load_strands, load_strands_arc_length, resample_strands_by_arclength  # noqa: F401
 from .rasterize import (InterpolateTriangleAttributes, barycentric_derivatives, cluster_mask_from_fragments,  # noqa: F401

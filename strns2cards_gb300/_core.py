@@ -498,6 +498,26 @@ def build_edges_from_triangles(tri):
     return edges[:E].copy(), e2t[:E].copy()
 
 
+def build_edges_device(tri, num_verts: int, edges=None, edge2tri=None, counts=None):
+    """Device: (edges (3T, 2), edge2tri (3T, 2), counts int64 (2,) = [num_edges, num_bad]) of a
+    CUDA int32 (T, 3) triangle tensor; the first num_edges rows are the edges.  No host
+    synchronisation."""
+    _arr(tri, _i32, 2, 3, "tri")
+    _cuda(tri, msg="build_edges_device: tri must be CUDA.")
+    T = tri.shape[0]
+    dev = tri.device
+    if edges is None:
+        edges = torch.empty((max(3 * T, 1), 2), dtype=_i32, device=dev)
+    if edge2tri is None:
+        edge2tri = torch.empty((max(3 * T, 1), 2), dtype=_i32, device=dev)
+    if counts is None:
+        counts = torch.zeros(2, dtype=torch.int64, device=dev)
+    ws = workspace(_lib.lib().s2c_build_edges_device_workspace_size(T, int(num_verts)), dev)
+    call("s2c_build_edges_device", T, ptr(tri), int(num_verts), ptr(edges), ptr(edge2tri), ptr(counts),
+         counts.data_ptr() + 8, ptr(ws), ws.numel(), _stream(tri))
+    return edges, edge2tri, counts
+
+
 # ---- strand curves (pystrns2cards.cpp:841-915) -----------------------------------------
 def compute_arclength(strands, arclength) -> None:
     _arr(strands, _f32, 3, 3, "strands")
@@ -622,6 +642,29 @@ def wisp_rotate(offsets, R_global, centre, a, b, a_out, b_out) -> None:
         raise RuntimeError("wisp_rotate: shapes do not match.")
     call("s2c_wisp_rotate", K, ptr(offsets), S, V, ptr(R_global), ptr(centre), ptr(a), ptr(b), ptr(a_out), ptr(b_out),
          _stream(a))
+
+
+def align_strands_max_points() -> int:
+    return int(_lib.lib().s2c_align_strands_max_points())
+
+
+def align_strands(strands, offsets, R_global, centre, t_dst, beta, handles, aligned) -> None:
+    """Smoothing, wisp rotation, frames and skinning of every strand in one launch (the part
+    of align_wisps after its per-wisp frames)."""
+    _arr(strands, _f32, 3, 3, "strands")
+    _arr(offsets, _i32, 1, name="offsets")
+    _arr(R_global, _f32, 3, 3, "R_global")
+    _arr(centre, _f32, 2, 3, "centre")
+    _arr(handles, _f32, 3, 3, "handles")
+    _arr(aligned, _f32, 3, 3, "aligned")
+    _cuda(strands, offsets, R_global, centre, handles, aligned, msg="align_strands: All input tensors must be CUDA.")
+    S, V, _ = strands.shape
+    K = offsets.shape[0] - 1
+    if K < 0 or R_global.shape[0] != K or centre.shape[0] != K or tuple(handles.shape) != (S, V, 3) \
+            or tuple(aligned.shape) != (S, V, 3):
+        raise RuntimeError("align_strands: shapes do not match.")
+    call("s2c_align_strands", S, V, ptr(strands), K, ptr(offsets), ptr(R_global), ptr(centre), _vec3(t_dst),
+         float(beta), ptr(handles), ptr(aligned), _stream(strands))
 
 
 # ---- strand ingest (pystrns2cards.cpp:788-839) -----------------------------------------

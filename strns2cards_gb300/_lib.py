@@ -78,6 +78,10 @@ SIGNATURES = {
     "s2c_strand_frames": ([c_i, c_i, vp, vp, vp, vp, vp, vp, vp, c_i64, vp, vp], c_i),
     "s2c_wisp_frames": ([c_i, vp, c_i64, c_i, vp, vp, vp, vp, vp, vp, vp, vp], c_i),
     "s2c_wisp_rotate": ([c_i, vp, c_i64, c_i, vp, vp, vp, vp, vp, vp, vp], c_i),
+    "s2c_align_strands_max_points": ([], c_i),
+    "s2c_build_edges_device_workspace_size": ([c_i, c_i], c_sz),
+    "s2c_build_edges_device": ([c_i, vp, c_i, vp, vp, vp, vp, vp, c_sz, vp], c_i),
+    "s2c_align_strands": ([c_i64, c_i, vp, c_i, vp, vp, vp, vp, c_f, vp, vp, vp], c_i),
     "s2c_build_edges_from_triangles": ([c_i, vp, vp, vp, i64p], c_i),
     "s2c_load_strands": ([ctypes.c_char_p, ctypes.POINTER(vp), i64p, i64p], c_i),
     "s2c_strands_take": ([vp, vp, vp], c_i),

@@ -14,6 +14,7 @@
 
 #include "common.cuh"
 #include "scan.cuh"
+#include "strand_sums.cuh"
 
 namespace s2c {
 namespace {
@@ -35,37 +36,6 @@ struct CurveArgs {
     float* out;
     float beta;
 };
-
-// arclength of one strand (points x[0..V), xyz interleaved) into arc[0..V), by one warp:
-// segment lengths, then an inclusive warp scan per 32-point chunk carried across chunks.
-__device__ __forceinline__ void warp_arclength(const float* x, int V, float* arc, int lane) {
-    float carry = 0.f;
-    for (int base = 0; base < V; base += 32) {
-        const int i = base + lane;
-        float d = 0.f;
-        if (i > 0 && i < V) {
-            const float dx = __fsub_rn(x[3 * i], x[3 * i - 3]);
-            const float dy = __fsub_rn(x[3 * i + 1], x[3 * i - 2]);
-            const float dz = __fsub_rn(x[3 * i + 2], x[3 * i - 1]);
-            d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-        }
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float t = __shfl_up_sync(0xffffffffu, d, o);
-            if (lane >= o) d = __fadd_rn(d, t);
-        }
-        // the scan's sums take different rounding paths per lane; a running maximum (exact,
-        // and a NaN stays NaN) keeps the arclength non-decreasing, which the pair windows of
-        // curve_kernel rely on
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const float t = __shfl_up_sync(0xffffffffu, d, o);
-            if (lane >= o && t > d) d = t;
-        }
-        if (i < V) arc[i] = __fadd_rn(carry, d);
-        carry = __fadd_rn(carry, __shfl_sync(0xffffffffu, d, 31));
-    }
-}
 
 template <bool kSkin>
 __global__ void __launch_bounds__(kCurveThreads) curve_kernel(CurveArgs a) {
@@ -115,56 +85,15 @@ __global__ void __launch_bounds__(kCurveThreads) curve_kernel(CurveArgs a) {
             const int sl = p / V;
             const int i = p - sl * V;
             const int b = sl * V;
-            const float si = sarc[p];
-            float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, sw = 0.f;
-            float xi0 = 0.f, xi1 = 0.f, xi2 = 0.f;
-            if (kSkin) { xi0 = X[3 * p]; xi1 = X[3 * p + 1]; xi2 = X[3 * p + 2]; }
-            // With the arclength computed here (non-decreasing along the strand) the points
-            // within the cutoff of point i form one run around i: walk out to its ends and sum
-            // over it in ascending order, the same terms in the same order as the full loop.
-            // A caller's arclength, or a non-finite one, takes the full loop.
-            int jlo = 0, jhi = V - 1;
-            if (!a.arc && isfinite(si) && isfinite(sarc[b + V - 1])) {
-                jlo = i;
-                while (jlo > 0 && !(fabsf(__fsub_rn(si, sarc[b + jlo - 1])) > cutoff)) --jlo;
-                jhi = i;
-                while (jhi < V - 1 && !(fabsf(__fsub_rn(si, sarc[b + jhi + 1])) > cutoff)) ++jhi;
-            }
-            for (int j = jlo; j <= jhi; ++j) {
-                const float dist = fabsf(__fsub_rn(si, sarc[b + j]));
-                if (dist > cutoff) continue;
-                const float w = expf(__fmul_rn(-__fmul_rn(dist, dist), inv_beta2));
-                const int q = b + j;
-                if (kSkin) {
-                    const float l0 = __fsub_rn(xi0, Hh[3 * q]);
-                    const float l1 = __fsub_rn(xi1, Hh[3 * q + 1]);
-                    const float l2 = __fsub_rn(xi2, Hh[3 * q + 2]);
-                    const float* r = RR + 9 * q;
-                    const float r0 = __fmaf_rn(r[2], l2, __fmaf_rn(r[1], l1, __fmul_rn(r[0], l0)));
-                    const float r1 = __fmaf_rn(r[5], l2, __fmaf_rn(r[4], l1, __fmul_rn(r[3], l0)));
-                    const float r2 = __fmaf_rn(r[8], l2, __fmaf_rn(r[7], l1, __fmul_rn(r[6], l0)));
-                    acc0 = __fmaf_rn(w, __fadd_rn(r0, Cc[3 * q]), acc0);
-                    acc1 = __fmaf_rn(w, __fadd_rn(r1, Cc[3 * q + 1]), acc1);
-                    acc2 = __fmaf_rn(w, __fadd_rn(r2, Cc[3 * q + 2]), acc2);
-                } else {
-                    acc0 = __fmaf_rn(w, X[3 * q], acc0);
-                    acc1 = __fmaf_rn(w, X[3 * q + 1], acc1);
-                    acc2 = __fmaf_rn(w, X[3 * q + 2], acc2);
-                }
-                sw = __fadd_rn(sw, w);
-            }
+            float o3[3];
+            if (kSkin)
+                skin_point(X + 3 * b, sarc + b, Hh + 3 * b, Cc + 3 * b, RR + 9 * b, V, i, cutoff, inv_beta2, !a.arc, o3);
+            else
+                smooth_point(X + 3 * b, sarc + b, V, i, cutoff, inv_beta2, !a.arc, o3);
             float* o = a.out + 3 * (p0 + p);
-            if (kSkin) {
-                const bool ok = sw > 1e-8f;
-                o[0] = ok ? __fdiv_rn(acc0, sw) : xi0;
-                o[1] = ok ? __fdiv_rn(acc1, sw) : xi1;
-                o[2] = ok ? __fdiv_rn(acc2, sw) : xi2;
-            } else {
-                const bool ok = sw > 1e-6f;
-                o[0] = ok ? __fdiv_rn(acc0, sw) : 0.f;
-                o[1] = ok ? __fdiv_rn(acc1, sw) : 0.f;
-                o[2] = ok ? __fdiv_rn(acc2, sw) : 0.f;
-            }
+            o[0] = o3[0];
+            o[1] = o3[1];
+            o[2] = o3[2];
         }
         __syncthreads();
     }

@@ -12,6 +12,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "strand_sums.cuh"
 
 namespace s2c {
 namespace {
@@ -157,20 +158,122 @@ struct FrameArgs {
 constexpr int kFrameThreads = 256;
 constexpr int kFrameWarps = kFrameThreads / 32;
 
+__device__ __forceinline__ V3 shfl_down3(V3 v, int d) {
+    return v3(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
+              __shfl_down_sync(0xffffffffu, v.z, d));
+}
+__device__ __forceinline__ float shfl_f(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+// State a warp carries from one 32-point chunk of a strand to the next.
+struct FrameCarry {
+    V3 n0, b0;       // the root frame (tangent_frame of the root tangent)
+    V3 nd, bd;       // the root frame turned onto t_dst (minimal rotation)
+    V3 n_prev;       // the normal at the point before the chunk
+    V3 p_last, t_last;
+    float arc;       // arclength at the point before the chunk
+};
+
+struct FramePoint {
+    V3 p, t, n, b;
+    float arc;
+};
+
+__device__ __forceinline__ void frame_root(const float* p, int V, V3 td, bool want_dst, FrameCarry& cy) {
+    const V3 t0 = tangent_at(p, 0, V);
+    tangent_frame(t0, cy.n0, cy.b0);
+    cy.nd = cy.n0;
+    cy.bd = cy.b0;
+    if (want_dst) {
+        float Ra[9];
+        minimal_rotation(t0, td, Ra);
+        cy.nd = matvec(Ra, cy.n0);
+        cy.bd = matvec(Ra, cy.b0);
+    }
+    cy.n_prev = cy.n0;
+    cy.p_last = ld3(p);
+    cy.t_last = t0;
+    cy.arc = 0.f;
+}
+
+// One 32-point chunk (points c0 + lane) of the rotation-minimising frame of the strand p
+// (curve_utils.py:104-165), for the whole warp.  The reference steps the normal point by
+// point: n_i = normalize(H2_i H1_i n_{i-1}), H1_i = I - 2 v1 v1^T / c1 (v1 = x_i - x_{i-1}) and
+// H2_i = I - 2 v2 v2^T / c2 (v2 = t_i - H1_i t_{i-1}), c clamped below at 1e-8.  Neither map
+// depends on the normal and each normalisation only scales by a positive number, so
+// n_i = normalize(M_i ... M_c0 n_{c0-1}) with M_i = H2_i H1_i: every lane builds its M_i and
+// a warp scan forms the prefix products (later factors on the left).  Tangents as the
+// reference's (x_{i+1} - x_i) + (x_i - x_{i-1}), one-sided at the ends, normalised; the
+// binormal normalize(t_i x n_i) (b_0 from tangent_frame); the arclength a warp scan of the
+// segment lengths.  Lanes past the strand's end return zeros.
+__device__ __forceinline__ FramePoint frame_chunk(const float* p, int V, int c0, int lane, FrameCarry& cy) {
+    const int i = c0 + lane;
+    const bool valid = i < V;
+    const V3 z = v3(0.f, 0.f, 0.f);
+    const V3 pi = valid ? ld3(p + 3 * i) : z;
+    V3 pn = shfl_down3(pi, 1), pp = shfl_up3(pi, 1);
+    if (lane == 31 && i + 1 < V) pn = ld3(p + 3 * (i + 1));
+    if (lane == 0) pp = cy.p_last;
+    V3 t = z;
+    if (valid) {
+        if (i + 1 < V) t = add(t, sub(pn, pi));
+        if (i > 0) t = add(t, sub(pi, pp));
+        t = unit(t);
+    }
+    V3 tp = shfl_up3(t, 1);
+    if (lane == 0) tp = cy.t_last;
+    M3 P = m3_identity();
+    float arc = 0.f;
+    if (valid && i > 0) {
+        const V3 v1 = sub(pi, pp);
+        const float c1 = fmaxf(dot(v1, v1), 1e-8f);
+        const M3 H1 = householder(v1, 2.f / c1);
+        const V3 v2 = sub(t, m3_vec(H1, tp));
+        const float c2 = fmaxf(dot(v2, v2), 1e-8f);
+        P = m3_mul(householder(v2, 2.f / c2), H1);
+        arc = norm(v1);
+    }
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        M3 Q;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Q.m[k] = __shfl_up_sync(0xffffffffu, P.m[k], d);
+        const float ua = __shfl_up_sync(0xffffffffu, arc, d);
+        if (lane >= d) {
+            P = m3_mul(P, Q);
+            arc += ua;
+        }
+    }
+    arc += cy.arc;
+    V3 n = cy.n0, b = cy.b0;
+    if (i > 0) {
+        n = unit(m3_vec(P, cy.n_prev));
+        b = unit(cross(t, n));
+    }
+    if (!valid) {
+        n = z;
+        b = z;
+    }
+    cy.n_prev = shfl3(n, 31);
+    cy.arc = shfl_f(arc, 31);
+    cy.p_last = shfl3(pi, 31);
+    cy.t_last = shfl3(t, 31);
+    return FramePoint{pi, t, n, b, arc};
+}
+
+// [t_dst n_dst b_dst] [t n b]^T, row-major
+__device__ __forceinline__ void align_rotation(V3 td, V3 nd, V3 bd, V3 t, V3 n, V3 b, float R[9]) {
+    const float dc[3][3] = {{td.x, nd.x, bd.x}, {td.y, nd.y, bd.y}, {td.z, nd.z, bd.z}};
+    const float sc[3][3] = {{t.x, n.x, b.x}, {t.y, n.y, b.y}, {t.z, n.z, b.z}};
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr)
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc)
+            R[3 * rr + cc] = (dc[rr][0] * sc[cc][0] + dc[rr][1] * sc[cc][1]) + dc[rr][2] * sc[cc][2];
+}
+
 // compute_bishop_frame (curve_utils.py:104-165) + compute_alignment_rotation (:273-308) +
-// compute_aligned_strands (:243-271): one warp per strand, one lane per point.
-//
-// The reference steps the normal point by point: n_i = normalize(H2_i H1_i n_{i-1}) with the
-// reflections H1_i = I - 2 v1 v1^T / c1 (v1 = x_i - x_{i-1}) and H2_i = I - 2 v2 v2^T / c2
-// (v2 = t_i - H1_i t_{i-1}), c clamped below at 1e-8.  Neither reflection depends on the
-// normal, and each normalisation only scales by a positive number, so
-// n_i = normalize(M_i M_{i-1} ... M_1 n_0) with M_i = H2_i H1_i: every lane builds its M_i,
-// a warp scan forms the prefix products (later factors on the left) and a carry joins the
-// 32-point chunks (rescaled by its largest entry, which leaves the directions unchanged).
-// Tangents, the root frame (tangent_frame), the binormals b_i = normalize(t_i x n_i) (b_0
-// from tangent_frame), the rotations [t_dst n_dst b_dst][t n b]^T and the canonical
-// handles (arclength by a warp scan of the segment lengths) follow per lane; each warp
-// writes its 32 points' outputs through shared memory as contiguous runs.
+// compute_aligned_strands (:243-271): one warp per strand, one lane per point (frame_chunk);
+// each warp writes its 32 points' outputs through shared memory as contiguous runs.
 __global__ void __launch_bounds__(kFrameThreads) strand_frames_kernel(FrameArgs a) {
     __shared__ float sbuf[kFrameWarps][32 * 9];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -180,95 +283,25 @@ __global__ void __launch_bounds__(kFrameThreads) strand_frames_kernel(FrameArgs 
     const int64_t nwarps = (int64_t)gridDim.x * kFrameWarps;
     for (int64_t s = (int64_t)blockIdx.x * kFrameWarps + warp; s < a.N; s += nwarps) {
         const float* p = a.strands + s * V * 3;
-        // the root frame and the destination frame at the root
-        const V3 t0 = tangent_at(p, 0, V);
-        V3 n0, b0;
-        tangent_frame(t0, n0, b0);
-        V3 nd = n0, bd = b0;
-        if (a.R) {
-            float Ra[9];
-            minimal_rotation(t0, td, Ra);
-            nd = matvec(Ra, n0);
-            bd = matvec(Ra, b0);
-        }
+        FrameCarry cy;
+        frame_root(p, V, td, a.R != nullptr, cy);
         const V3 root = a.roots ? ld3(a.roots + a.roots_stride * s) : ld3(p);
-        M3 carry = m3_identity();
-        float carry_arc = 0.f;
-        V3 p_last = ld3(p), t_last = t0;
         for (int c0 = 0; c0 < V; c0 += 32) {
-            const int i = c0 + lane;
-            const bool valid = i < V;
-            const V3 pi = valid ? ld3(p + 3 * i) : v3(0.f, 0.f, 0.f);
-            const V3 t = valid ? tangent_at(p, i, V) : v3(0.f, 0.f, 0.f);
-            V3 pp = shfl_up3(pi, 1), tp = shfl_up3(t, 1);
-            if (lane == 0) {
-                pp = p_last;
-                tp = t_last;
-            }
-            M3 P = m3_identity();
-            float seg = 0.f;
-            if (valid && i > 0) {
-                const V3 v1 = sub(pi, pp);
-                const float c1 = fmaxf(dot(v1, v1), 1e-8f);
-                const M3 H1 = householder(v1, 2.f / c1);
-                const V3 v2 = sub(t, m3_vec(H1, tp));
-                const float c2 = fmaxf(dot(v2, v2), 1e-8f);
-                P = m3_mul(householder(v2, 2.f / c2), H1);
-                seg = norm(v1);
-            }
-            float arc = seg;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1) {
-                M3 Q;
-#pragma unroll
-                for (int k = 0; k < 9; ++k) Q.m[k] = __shfl_up_sync(0xffffffffu, P.m[k], d);
-                const float ua = __shfl_up_sync(0xffffffffu, arc, d);
-                if (lane >= d) {
-                    P = m3_mul(P, Q);
-                    arc += ua;
-                }
-            }
-            P = m3_mul(P, carry);
-            arc += carry_arc;
-            V3 n = n0, b = b0;
-            if (i > 0) {
-                n = unit(m3_vec(P, n0));
-                b = unit(cross(t, n));
-            }
+            const FramePoint f = frame_chunk(p, V, c0, lane, cy);
             const int nitems = min(32, V - c0);
             const int64_t o = s * V + c0;
-            if (a.T) warp_store<3>(wbuf, {t.x, t.y, t.z}, a.T + 3 * o, nitems, lane);
-            if (a.Nn) warp_store<3>(wbuf, {n.x, n.y, n.z}, a.Nn + 3 * o, nitems, lane);
-            if (a.Bn) warp_store<3>(wbuf, {b.x, b.y, b.z}, a.Bn + 3 * o, nitems, lane);
+            if (a.T) warp_store<3>(wbuf, {f.t.x, f.t.y, f.t.z}, a.T + 3 * o, nitems, lane);
+            if (a.Nn) warp_store<3>(wbuf, {f.n.x, f.n.y, f.n.z}, a.Nn + 3 * o, nitems, lane);
+            if (a.Bn) warp_store<3>(wbuf, {f.b.x, f.b.y, f.b.z}, a.Bn + 3 * o, nitems, lane);
             if (a.R) {
-                const float dc[3][3] = {{td.x, nd.x, bd.x}, {td.y, nd.y, bd.y}, {td.z, nd.z, bd.z}};
-                const float sc[3][3] = {{t.x, n.x, b.x}, {t.y, n.y, b.y}, {t.z, n.z, b.z}};
                 float R[9];
-#pragma unroll
-                for (int rr = 0; rr < 3; ++rr)
-#pragma unroll
-                    for (int cc = 0; cc < 3; ++cc)
-                        R[3 * rr + cc] = (dc[rr][0] * sc[cc][0] + dc[rr][1] * sc[cc][1]) + dc[rr][2] * sc[cc][2];
+                align_rotation(td, cy.nd, cy.bd, f.t, f.n, f.b, R);
                 warp_store<9>(wbuf, R, a.R + 9 * o, nitems, lane);
             }
             if (a.canon) {
-                const V3 cn = add(mul(td, arc), root);
+                const V3 cn = add(mul(td, f.arc), root);
                 warp_store<3>(wbuf, {cn.x, cn.y, cn.z}, a.canon + 3 * o, nitems, lane);
             }
-            // carry into the next chunk: the product through lane 31, rescaled
-            M3 last;
-            float mx = 0.f;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) {
-                last.m[k] = __shfl_sync(0xffffffffu, P.m[k], 31);
-                mx = fmaxf(mx, fabsf(last.m[k]));
-            }
-            const float inv = mx > 0.f ? 1.f / mx : 1.f;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) carry.m[k] = last.m[k] * inv;
-            carry_arc = __shfl_sync(0xffffffffu, arc, 31);
-            p_last = shfl3(pi, 31);
-            t_last = shfl3(t, 31);
         }
     }
 }
@@ -485,9 +518,42 @@ __global__ void __launch_bounds__(kWispThreads) wisp_frames_kernel(int num_wisps
     st3(centre + 3 * w, c);
 }
 
+// R (x - c), the expression both wisp_rotate_kernel and align_strands_kernel use
+__device__ __forceinline__ V3 rotate_about(const float R[9], V3 c, V3 x) {
+    x = sub(x, c);
+    return v3((R[0] * x.x + R[1] * x.y) + R[2] * x.z, (R[3] * x.x + R[4] * x.y) + R[5] * x.z,
+              (R[6] * x.x + R[7] * x.y) + R[8] * x.z);
+}
+
+// the wisp holding strand s (binary search over the offsets by lane 0, broadcast), or -1;
+// R, c receive its frame (identity and 0 for no wisp)
+__device__ __forceinline__ int wisp_of_strand(int64_t s, int num_wisps, const int32_t* __restrict__ offs,
+                                              const float* __restrict__ Rg, const float* __restrict__ centre,
+                                              int lane, float R[9], V3& c) {
+    int w = -1;
+    if (lane == 0 && num_wisps > 0 && s >= offs[0] && s < offs[num_wisps]) {
+        int lo = 0, hi = num_wisps - 1;   // last w with offs[w] <= s
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (offs[mid] <= s) lo = mid; else hi = mid - 1;
+        }
+        if (offs[lo] <= s && s < offs[lo + 1]) w = lo;
+    }
+    w = __shfl_sync(0xffffffffu, w, 0);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) R[k] = (k % 4 == 0) ? 1.f : 0.f;
+    c = v3(0.f, 0.f, 0.f);
+    if (w >= 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) R[k] = __ldg(Rg + 9 * w + k);
+        c = ld3(centre + 3 * w);
+    }
+    return w;
+}
+
 // a_out = R_w (a - centre_w) and b_out likewise for every point of every strand, w the wisp
-// whose offsets range holds the strand: a warp per strand (lane 0 finds the wisp by binary
-// search over the offsets, lanes over the points).
+// whose offsets range holds the strand (a strand of no wisp is copied unchanged): a warp per
+// strand, lanes over the points.
 __global__ void __launch_bounds__(256) wisp_rotate_kernel(int64_t num_strands, int V, int num_wisps,
                                                           const int32_t* __restrict__ offs,
                                                           const float* __restrict__ Rg,
@@ -497,31 +563,99 @@ __global__ void __launch_bounds__(256) wisp_rotate_kernel(int64_t num_strands, i
     const int lane = threadIdx.x & 31;
     const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
     for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < num_strands; s += nw) {
-        int w = -1;
-        if (lane == 0 && num_wisps > 0 && s >= offs[0] && s < offs[num_wisps]) {
-            int lo = 0, hi = num_wisps - 1;   // last w with offs[w] <= s
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (offs[mid] <= s) lo = mid; else hi = mid - 1;
-            }
-            if (offs[lo] <= s && s < offs[lo + 1]) w = lo;
-        }
-        w = __shfl_sync(0xffffffffu, w, 0);
-        float R[9] = {1.f, 0.f, 0.f, 0.f, 1.f, 0.f, 0.f, 0.f, 1.f};
-        V3 c = v3(0.f, 0.f, 0.f);
-        if (w >= 0) {   // a strand of no wisp is copied unchanged
-#pragma unroll
-            for (int k = 0; k < 9; ++k) R[k] = __ldg(Rg + 9 * w + k);
-            c = ld3(centre + 3 * w);
-        }
+        float R[9];
+        V3 c;
+        const int w = wisp_of_strand(s, num_wisps, offs, Rg, centre, lane, R, c);
         const int64_t o = s * V;
         for (int i = lane; i < V; i += 32) {
-            const V3 x = sub(ld3(a + 3 * (o + i)), c), y = sub(ld3(b + 3 * (o + i)), c);
-            st3(ao + 3 * (o + i), v3((R[0] * x.x + R[1] * x.y) + R[2] * x.z, (R[3] * x.x + R[4] * x.y) + R[5] * x.z,
-                                     (R[6] * x.x + R[7] * x.y) + R[8] * x.z));
-            st3(bo + 3 * (o + i), v3((R[0] * y.x + R[1] * y.y) + R[2] * y.z, (R[3] * y.x + R[4] * y.y) + R[5] * y.z,
-                                     (R[6] * y.x + R[7] * y.y) + R[8] * y.z));
+            const V3 x = ld3(a + 3 * (o + i)), y = ld3(b + 3 * (o + i));
+            st3(ao + 3 * (o + i), w >= 0 ? rotate_about(R, c, x) : x);
+            st3(bo + 3 * (o + i), w >= 0 ? rotate_about(R, c, y) : y);
         }
+    }
+}
+
+// align_wisps after the per-wisp frames (curve_utils.py:487-606), one warp per strand with the
+// strand staged in shared memory: smoothing (the handle strand, written out), rotation of
+// the strand and its handle into the wisp frame, rotation-minimising frames of the rotated
+// handle (frame_chunk) with its alignment rotations and canonical handles, and skinning of
+// the rotated strand.  The same device code as smooth_strands, wisp_rotate, strand_frames
+// and skinning, in the same order, so the result equals that composition bit for bit while
+// only the strands are read and the handles and aligned strands written.
+constexpr int kAlignFloatsPerPoint = 19;   // x 3, handle 3, R 9, canonical 3, arclength 1
+constexpr int kAlignSmemMax = 96 * 1024;
+
+struct AlignArgs {
+    int64_t N;
+    int V;
+    const float* strands;
+    int num_wisps;
+    const int32_t* offs;
+    const float* Rg;
+    const float* centre;
+    V3 td;
+    float beta;
+    float* handles;   // (N, V, 3): the smoothed strands before alignment
+    float* aligned;   // (N, V, 3)
+};
+
+__global__ void __launch_bounds__(256) align_strands_kernel(AlignArgs a) {
+    extern __shared__ float asm_[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps_cta = blockDim.x >> 5;
+    const int V = a.V;
+    float* sx = asm_ + (size_t)warp * kAlignFloatsPerPoint * V;
+    float* sh = sx + 3 * V;
+    float* sR = sh + 3 * V;
+    float* sc = sR + 9 * V;
+    float* sarc = sc + 3 * V;
+    const float inv_beta2 = __fdiv_rn(1.0f, __fmul_rn(a.beta, a.beta));
+    const float cutoff = __fmul_rn(3.0f, a.beta);
+    const int64_t nw = (int64_t)gridDim.x * nwarps_cta;
+    for (int64_t s = (int64_t)blockIdx.x * nwarps_cta + warp; s < a.N; s += nw) {
+        float R[9];
+        V3 c;
+        const int w = wisp_of_strand(s, a.num_wisps, a.offs, a.Rg, a.centre, lane, R, c);
+        const int64_t o = s * V;
+        for (int k = lane; k < 3 * V; k += 32) sx[k] = __ldg(a.strands + 3 * o + k);
+        __syncwarp();
+        warp_arclength(sx, V, sarc, lane);
+        __syncwarp();
+        // the handle strand: smoothed, written out, rotated into the wisp frame
+        for (int i = lane; i < V; i += 32) {
+            float h3[3];
+            smooth_point(sx, sarc, V, i, cutoff, inv_beta2, true, h3);
+            const V3 h = v3(h3[0], h3[1], h3[2]);
+            st3(a.handles + 3 * (o + i), h);
+            st3(sh + 3 * i, w >= 0 ? rotate_about(R, c, h) : h);
+        }
+        __syncwarp();
+        for (int i = lane; i < V; i += 32) {
+            const V3 x = ld3(sx + 3 * i);
+            st3(sx + 3 * i, w >= 0 ? rotate_about(R, c, x) : x);
+        }
+        __syncwarp();
+        // frames of the rotated handle: rotations and canonical handles
+        FrameCarry cy;
+        frame_root(sh, V, a.td, true, cy);
+        const V3 root = ld3(sx);
+        for (int c0 = 0; c0 < V; c0 += 32) {
+            const FramePoint f = frame_chunk(sh, V, c0, lane, cy);
+            const int i = c0 + lane;
+            if (i < V) {
+                align_rotation(a.td, cy.nd, cy.bd, f.t, f.n, f.b, sR + 9 * i);
+                st3(sc + 3 * i, add(mul(a.td, f.arc), root));
+            }
+        }
+        __syncwarp();
+        warp_arclength(sx, V, sarc, lane);
+        __syncwarp();
+        for (int i = lane; i < V; i += 32) {
+            float o3[3];
+            skin_point(sx, sarc, sh, sc, sR, V, i, cutoff, inv_beta2, true, o3);
+            st3(a.aligned + 3 * (o + i), v3(o3[0], o3[1], o3[2]));
+        }
+        __syncwarp();
     }
 }
 
@@ -581,5 +715,43 @@ extern "C" S2C_API s2c_status s2c_wisp_rotate(int num_wisps, const int32_t* offs
     wisp_rotate_kernel<<<grid_for(num_strands, 8, (int64_t)num_sms() * 16), 256, 0, (cudaStream_t)stream>>>(
         num_strands, V, num_wisps, offsets, R_global, centre, a, b, a_out, b_out);
     S2C_CHECK_LAUNCH("wisp_rotate_kernel");
+    return S2C_OK;
+}
+
+extern "C" S2C_API int s2c_align_strands_max_points(void) {
+    return kAlignSmemMax / (kAlignFloatsPerPoint * 4);
+}
+
+extern "C" S2C_API s2c_status s2c_align_strands(int64_t num_strands, int V, const float* strands, int num_wisps,
+                                                const int32_t* offsets, const float* R_global, const float* centre,
+                                                const float* t_dst, float beta, float* handles, float* aligned,
+                                                s2c_stream stream) {
+    S2C_REQUIRE(num_strands >= 0 && num_wisps >= 0 && V >= 2, "align_strands: bad sizes");
+    S2C_REQUIRE(V <= s2c_align_strands_max_points(), "align_strands: strands of %d points exceed the staged limit of %d",
+                V, s2c_align_strands_max_points());
+    if (num_strands == 0) return S2C_OK;
+    S2C_REQUIRE(strands && t_dst && handles && aligned && (num_wisps == 0 || (offsets && R_global && centre)),
+                "align_strands: null pointer");
+    AlignArgs a;
+    a.N = num_strands;
+    a.V = V;
+    a.strands = strands;
+    a.num_wisps = num_wisps;
+    a.offs = offsets;
+    a.Rg = R_global;
+    a.centre = centre;
+    a.td = v3(t_dst[0], t_dst[1], t_dst[2]);
+    a.beta = beta;
+    a.handles = handles;
+    a.aligned = aligned;
+    const size_t per_warp = (size_t)kAlignFloatsPerPoint * 4 * V;
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, kAlignSmemMax / per_warp));
+    const size_t smem = per_warp * warps;
+    if (smem > 48 * 1024)   // per call: the attribute belongs to the current device
+        cudaFuncSetAttribute(align_strands_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int per_sm = std::max(1, (int)(200 * 1024 / smem));
+    align_strands_kernel<<<grid_for(num_strands, warps, (int64_t)num_sms() * per_sm), warps * 32, smem,
+                           (cudaStream_t)stream>>>(a);
+    S2C_CHECK_LAUNCH("align_strands_kernel");
     return S2C_OK;
 }

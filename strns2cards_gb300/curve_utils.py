@@ -8,10 +8,11 @@ aligners ``align_wisps`` / ``align_wisp`` (``:376-607``) and ``strands_to_tube``
 arclength of the strands it stages instead of reading a separately computed tensor.
 The rotation-minimising frame is one thread per strand walking the double-reflection
 recurrence (the reference loops over the points in Python); its alignment rotations and
-canonical handles come out of the same pass.  ``align_wisps`` is five launches for all
-wisps together -- smoothing, per-wisp frames (one CTA per wisp, an FP64 3x3 eigen-solve in
-place of the host SVD), rotation, frames + canonical handles, skinning -- with no host
-synchronisation (the reference runs a Python loop over wisps with a host SVD each).
+canonical handles come out of the same pass.  ``align_wisps`` is two launches for all
+wisps together -- the per-wisp frames (one CTA per wisp, a 3x3 eigen-solve in place of the
+host SVD), then smoothing, rotation, frames + canonical handles and skinning fused, one
+warp per strand -- with no host synchronisation (the reference runs a Python loop over
+wisps with a host SVD each, and a Python loop over the points for the frames).
 """
 from __future__ import annotations
 
@@ -156,8 +157,8 @@ def align_wisps(wisps: List, beta: float) -> Tuple[torch.Tensor, torch.Tensor, t
     ``wisps``: list of (N_i, V, 3) arrays (numpy or torch), one per wisp.  Returns the
     aligned strands (N, V, 3), the smoothed strands before alignment (N, V, 3) and the
     global index of each wisp's longest strand (int64), on the GPU.  The per-wisp frame
-    takes the least-variance axis of the wisp's centred roots from an FP64 eigen-solve of
-    their second moment (the reference's host SVD gives the same axis up to sign, and the
+    takes the least-variance axis of the wisp's centred roots from an FP32 Jacobi eigen-solve
+    of their second moment (the reference's host SVD gives the same axis up to sign, and the
     frame fixes the sign); below 3 strands the axes are the identity's, as there."""
     dev = torch.device("cuda")
     parts, sizes = [], []
@@ -180,7 +181,10 @@ def align_wisps(wisps: List, beta: float) -> Tuple[torch.Tensor, torch.Tensor, t
 
 def align_wisps_packed(strands: torch.Tensor, wisp_sizes: torch.Tensor, beta: float):
     """``align_wisps`` on strands already on the device, wisp w being the next
-    ``wisp_sizes[w]`` strands (a host tensor or sequence of sizes, all > 0)."""
+    ``wisp_sizes[w]`` strands (a host tensor or sequence of sizes, all > 0).  Two launches:
+    the per-wisp frames, then smoothing, rotation, frames and skinning of every strand
+    fused (strands longer than the fused kernel stages take the same steps one launch
+    each, with the same results)."""
     s = _check_strands(strands, "align_wisps")
     S, V, _ = s.shape
     sizes = torch.as_tensor(wisp_sizes, dtype=torch.int64).cpu()
@@ -193,19 +197,31 @@ def align_wisps_packed(strands: torch.Tensor, wisp_sizes: torch.Tensor, beta: fl
     offs = torch.zeros(K + 1, dtype=torch.int32)
     offs[1:] = torch.cumsum(sizes, 0).to(torch.int32)
     offs = offs.pin_memory().to(dev, non_blocking=True)
-    handles_orig = smooth_strands(s, beta)
     Rg = torch.empty((K, 3, 3), dtype=torch.float32, device=dev)
     centre = torch.empty((K, 3), dtype=torch.float32, device=dev)
     longest = torch.empty(K, dtype=torch.int32, device=dev)
     _core.wisp_frames(offs, s, WISP_T_DST, WISP_N_DST, WISP_B_DST, Rg, centre, longest)
+    if V <= _core.align_strands_max_points():
+        handles_orig, aligned = torch.empty_like(s), torch.empty_like(s)
+        _core.align_strands(s, offs, Rg, centre, WISP_T_DST, beta, handles_orig, aligned)
+    else:
+        aligned, handles_orig = _align_strands_unfused(s, offs, Rg, centre, beta)
+    return aligned, handles_orig, longest.to(torch.int64)
+
+
+def _align_strands_unfused(s, offs, Rg, centre, beta):
+    """The steps of the fused align_strands as separate launches: smoothing, rotation into
+    the wisp frames, frames + canonical handles of the rotated handles, skinning."""
+    S, V, _ = s.shape
+    handles_orig = smooth_strands(s, beta)
     s_rot, h_rot = torch.empty_like(s), torch.empty_like(s)
     _core.wisp_rotate(offs, Rg, centre, s, handles_orig, s_rot, h_rot)
     canon = torch.empty_like(s)
-    R_local = torch.empty((S, V, 3, 3), dtype=torch.float32, device=dev)
+    R_local = torch.empty((S, V, 3, 3), dtype=torch.float32, device=s.device)
     _core.strand_frames(h_rot, t_dst=WISP_T_DST, R=R_local, roots=s_rot[:, 0], canon=canon)
     aligned = torch.empty_like(s)
     _core.skinning(s_rot, None, h_rot, canon, R_local, aligned, beta)
-    return aligned, handles_orig, longest.to(torch.int64)
+    return aligned, handles_orig
 
 
 def align_wisp(strands: torch.Tensor, beta: float) -> Tuple[torch.Tensor, torch.Tensor, torch.Tensor]:

@@ -157,6 +157,37 @@ def test_align_wisps_against_oracle():
     assert torch.equal(a2, aligned) and torch.equal(h2, handles) and torch.equal(l2, longest)
 
 
+def test_fused_align_strands_equals_the_unfused_steps_bit_for_bit():
+    from strns2cards_gb300 import _core, curve_utils as cv
+    st, sizes = _wisp_case(3000, 48, 61, 8)
+    x = cu(st)
+    K = len(sizes)
+    offs = cu(np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32))
+    Rg = torch.empty((K, 3, 3), device="cuda")
+    cen = torch.empty((K, 3), device="cuda")
+    li = torch.empty(K, dtype=torch.int32, device="cuda")
+    _core.wisp_frames(offs, x, cv.WISP_T_DST, cv.WISP_N_DST, cv.WISP_B_DST, Rg, cen, li)
+    h, a = torch.empty_like(x), torch.empty_like(x)
+    _core.align_strands(x, offs, Rg, cen, cv.WISP_T_DST, 0.07, h, a)
+    a2, h2 = cv._align_strands_unfused(x, offs, Rg, cen, 0.07)
+    assert torch.equal(h, h2)
+    assert torch.equal(a, a2)
+
+
+def test_align_wisps_of_strands_too_long_to_fuse_against_oracle():
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    V = _core.align_strands_max_points() + 7
+    st, sizes = _wisp_case(12, V, 3, 9)
+    st = (st[:, :1] + 0.05 * (st - st[:, :1])).astype(np.float32)   # keep the strands a plausible length
+    wisps = np.split(st, np.cumsum(sizes)[:-1])
+    aligned, handles, longest = s2c.align_wisps(wisps, 0.002)
+    oa, oh, ol = O.align_wisps(wisps, 0.002)
+    assert np.array_equal(np_(longest), ol)
+    assert maxdiff(np_(handles), oh) <= 1e-5 * np.abs(oh).max()
+    assert maxdiff(np_(aligned), oa) <= 1e-3 * np.abs(oa).max()
+
+
 def test_align_wisps_one_wisp_equals_alone_and_in_the_mix():
     import strns2cards_gb300 as s2c
     st, sizes = _wisp_case(600, 24, 11, 5)
