@@ -477,10 +477,20 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
     const bool vec4 = (S & 3) == 0;
     const int n_heavy = (int)w.hdr[H_HEAVY];
     const int items = n_heavy + g.num_tiles;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    // the tile bitset starts cleared; each tile's write-out clears the words it reads
+    {
+        uint4* z4 = reinterpret_cast<uint4*>(sm_bits);
+        const int n4 = (S * rowstride) >> 2;
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) z4[i] = make_uint4(0, 0, 0, 0);
+        for (int i = (n4 << 2) + threadIdx.x; i < S * rowstride; i += blockDim.x) sm_bits[i] = 0u;
+    }
 
     for (;;) {
-        if (threadIdx.x == 0) s_item = (int)atomicAdd((unsigned long long*)(w.hdr + H_WORK), 1ull);
+        if (threadIdx.x == 0) {
+            s_item = (int)atomicAdd((unsigned long long*)(w.hdr + H_WORK), 1ull);
+            s_rec = 0;
+        }
         __syncthreads();
         const int item = s_item;
         __syncthreads();
@@ -525,29 +535,30 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             }
             continue;
         }
-        {
-            uint4* z4 = reinterpret_cast<uint4*>(sm_bits);
-            const int n4 = (S * rowstride) >> 2;
-            for (int i = threadIdx.x; i < n4; i += blockDim.x) z4[i] = make_uint4(0, 0, 0, 0);
-            for (int i = (n4 << 2) + threadIdx.x; i < S * rowstride; i += blockDim.x) sm_bits[i] = 0u;
-        }
-        __syncthreads();
         // Warps pull records from a shared counter.  Each warp loads 32 entries, scans their
         // run lengths and lets each lane decode one fragment: major offset i, minor offset
-        // popc(steps & ((1 << i) - 1)) in the run's direction.
-        if (threadIdx.x == 0) s_rec = 0;
-        __syncthreads();
-        for (;;) {
-            int r = 0;
-            if (lane == 0) r = atomicAdd(&s_rec, 1);
-            r = __shfl_sync(0xffffffffu, r, 0);
-            if (r >= nrec) break;
-            const int2 rc = w.sorted[rbeg + r];
+        // popc(steps & ((1 << i) - 1)) in the run's direction.  The next 32 entries (of this
+        // record, or the first of the warp's next record) are loaded before the current ones
+        // are decoded.
+        int r = 0;
+        if (lane == 0) r = atomicAdd(&s_rec, 1);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        int2 rc = r < nrec ? w.sorted[rbeg + r] : make_int2(0, 0);
+        uint2 e = (r < nrec && lane < rc.y) ? __ldcs(w.entries + rc.x + lane) : make_uint2(0, 0);
+        while (r < nrec) {
+            int rn = 0;
+            if (lane == 0) rn = atomicAdd(&s_rec, 1);
+            rn = __shfl_sync(0xffffffffu, rn, 0);
+            const int2 rcn = rn < nrec ? w.sorted[rbeg + rn] : make_int2(0, 0);
             for (int base = 0; base < rc.y; base += 32) {
-                uint2 e = make_uint2(0, 0);
+                uint2 en = make_uint2(0, 0);
+                if (base + 32 < rc.y) {
+                    if (base + 32 + lane < rc.y) en = __ldcs(w.entries + rc.x + base + 32 + lane);
+                } else if (rn < nrec && lane < rcn.y) {
+                    en = __ldcs(w.entries + rcn.x + lane);
+                }
                 int n = 0;
                 if (base + lane < rc.y) {
-                    e = __ldcs(w.entries + rc.x + base + lane);
                     n = (int)(e.y & 31) + 1;
                     if ((int)(e.x & 0xffff) >= 32 * S) n = 0;
                 }
@@ -604,7 +615,11 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
                         }
                     }
                 }
+                e = en;
             }
+            if (rc.y <= 0) e = (rn < nrec && lane < rcn.y) ? __ldcs(w.entries + rcn.x + lane) : make_uint2(0, 0);
+            r = rn;
+            rc = rcn;
         }
         __syncthreads();
         if (vec4) {
@@ -615,9 +630,13 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             int px = rem / G, sg = rem - px * G;
             const int dpx = drem / G, dsg = drem - dpx * G;
             for (; r < rows;) {
-                const uint32_t* src = sm_bits + (size_t)(4 * sg) * rowstride + r * TW + px;
-                __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W + px) * S + 4 * sg),
-                       make_int4((int)src[0], (int)src[rowstride], (int)src[2 * rowstride], (int)src[3 * rowstride]));
+                uint32_t* src = sm_bits + (size_t)(4 * sg) * rowstride + r * TW + px;
+                const int4 v = make_int4((int)src[0], (int)src[rowstride], (int)src[2 * rowstride], (int)src[3 * rowstride]);
+                src[0] = 0u;
+                src[rowstride] = 0u;
+                src[2 * rowstride] = 0u;
+                src[3 * rowstride] = 0u;
+                __stcs(reinterpret_cast<int4*>(bitset + (row0 + (int64_t)r * g.W + px) * S + 4 * sg), v);
                 r += dr;
                 px += dpx;
                 sg += dsg;
@@ -629,7 +648,10 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             for (int i = threadIdx.x; i < rows * per_row; i += blockDim.x) {
                 const int r = i / per_row, rem = i - r * per_row;
                 const int px = rem / S, sl = rem - px * S;
-                __stcs(bitset + (row0 + (int64_t)r * g.W) * S + rem, (int)sm_bits[(size_t)sl * rowstride + r * TW + px]);
+                uint32_t* src = sm_bits + (size_t)sl * rowstride + r * TW + px;
+                const int v = (int)*src;
+                *src = 0u;
+                __stcs(bitset + (row0 + (int64_t)r * g.W) * S + rem, v);
             }
         }
         __syncthreads();
