@@ -485,6 +485,25 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
         for (int i = threadIdx.x; i < n4; i += blockDim.x) z4[i] = make_uint4(0, 0, 0, 0);
         for (int i = (n4 << 2) + threadIdx.x; i < S * rowstride; i += blockDim.x) sm_bits[i] = 0u;
     }
+    // The 16-byte stores of a full tile: when a tile row's TW * G items divide the CTA's
+    // threads, thread t always takes pixel px and slot group sg (from t mod TW * G) and rows
+    // r0, r0 + dR, ... (dR = threads / (TW * G)), so its shared and global offsets are a base
+    // plus a fixed stride per store, computed once.  Other shapes and border tiles take the
+    // general loop.
+    const int G = S >> 2;
+    const bool fast_out = vec4 && TW * G <= kRasterThreads && kRasterThreads % (TW * G) == 0 &&
+                          (int64_t)TH * g.W * S < (1LL << 31);
+    int f_r0 = 0, f_soff = 0, f_goff = 0, f_dr = 1;
+    if (fast_out) {
+        const int rem = threadIdx.x % (TW * G);
+        const int px = rem / G, sg = rem - px * G;
+        f_r0 = threadIdx.x / (TW * G);
+        f_dr = kRasterThreads / (TW * G);
+        f_soff = (4 * sg) * rowstride + f_r0 * TW + px;
+        f_goff = (f_r0 * g.W + px) * S + 4 * sg;
+    }
+    const int f_sstep = f_dr * TW;
+    const int64_t f_gstep = (int64_t)f_dr * g.W * S;
 
     for (;;) {
         if (threadIdx.x == 0) {
@@ -510,9 +529,14 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
         const int nrec = w.nrec[tile];
         const int rbeg = w.roff[tile] - nrec;
         const int64_t row0 = ((int64_t)b * g.H + h0) * g.W + w0;
+        const bool full = fast_out && rows == TH && cols == TW;
         if (nrec == 0) {
-            // empty tile: zeros, row by row, 16 bytes per store where possible
-            if (vec4) {
+            // empty tile: zeros, 16 bytes per store where possible
+            if (full) {
+                int32_t* t = bitset + row0 * S + f_goff;
+                for (int r = f_r0; r < TH; r += f_dr, t += f_gstep)
+                    __stcs(reinterpret_cast<int4*>(t), make_int4(0, 0, 0, 0));
+            } else if (vec4) {
                 const int per_row = cols * (S >> 2);
                 int r = threadIdx.x / per_row, c = threadIdx.x - r * per_row;
                 const int dr = kRasterThreads / per_row, dc = kRasterThreads - dr * per_row;
@@ -622,9 +646,20 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             rc = rcn;
         }
         __syncthreads();
-        if (vec4) {
+        if (full) {
+            int32_t* t = bitset + row0 * S + f_goff;
+            uint32_t* src = sm_bits + f_soff;
+            for (int r = f_r0; r < TH; r += f_dr, t += f_gstep, src += f_sstep) {
+                const int4 v = make_int4((int)src[0], (int)src[rowstride], (int)src[2 * rowstride], (int)src[3 * rowstride]);
+                src[0] = 0u;
+                src[rowstride] = 0u;
+                src[2 * rowstride] = 0u;
+                src[3 * rowstride] = 0u;
+                __stcs(reinterpret_cast<int4*>(t), v);
+            }
+        } else if (vec4) {
             // thread -> (row, pixel, 16-byte slot group), advanced without divisions
-            const int G = S >> 2, per_row = cols * G;
+            const int per_row = cols * G;
             int r = threadIdx.x / per_row, rem = threadIdx.x - r * per_row;
             const int dr = kRasterThreads / per_row, drem = kRasterThreads - dr * per_row;
             int px = rem / G, sg = rem - px * G;
