@@ -459,7 +459,7 @@ __device__ __forceinline__ float4 shfl4(float4 v, int src) {
                        __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
 }
 
-__global__ void __launch_bounds__(256) aa_frag_kernel(AAArgs A, Mesh M, const uint32_t* __restrict__ prefix,
+__global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, Mesh M, const uint32_t* __restrict__ prefix,
                                                       const int64_t* __restrict__ total) {
     const int lane = threadIdx.x & 31;
     const int64_t BE = (int64_t)A.B * M.E;
