@@ -280,7 +280,7 @@ __device__ __forceinline__ void align_rotation(V3 td, V3 nd, V3 bd, V3 t, V3 n, 
 // compute_bishop_frame (curve_utils.py:104-165) + compute_alignment_rotation (:273-308) +
 // compute_aligned_strands (:243-271): one warp per strand, one lane per point (frame_chunk);
 // each warp writes its 32 points' outputs through shared memory as contiguous runs.
-__global__ void __launch_bounds__(kFrameThreads) strand_frames_kernel(FrameArgs a) {
+__global__ void __launch_bounds__(kFrameThreads, 4) strand_frames_kernel(FrameArgs a) {
     __shared__ float sbuf[kFrameWarps][32 * 9];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* wbuf = sbuf[warp];
@@ -605,7 +605,7 @@ struct AlignArgs {
     float* aligned;   // (N, V, 3)
 };
 
-__global__ void __launch_bounds__(256) align_strands_kernel(AlignArgs a) {
+__global__ void __launch_bounds__(256, 4) align_strands_kernel(AlignArgs a) {
     extern __shared__ float asm_[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int nwarps_cta = blockDim.x >> 5;
