@@ -10,9 +10,13 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "s2c.h"
 
 namespace s2c {
+
+constexpr int kMaxDevices = 64;   // per-device launch caches (device index mod 64)
 
 // ---- status / errors -------------------------------------------------------------
 void set_error(const char* fmt, ...);
@@ -27,13 +31,24 @@ s2c_status cuda_status(cudaError_t e, const char* what);
         if (!(cond)) { ::s2c::set_error(__VA_ARGS__); return S2C_ERR_INVALID; } \
     } while (0)
 
+// the calling thread's current device, as an index into the per-device caches below
+inline int current_device_slot() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev & (kMaxDevices - 1);
+}
+
+// SM count of the current device (cached per device)
 inline int num_sms() {
-    static int n = 0;
+    static std::atomic<int> cache[kMaxDevices];
+    const int slot = current_device_slot();
+    int n = cache[slot].load(std::memory_order_relaxed);
     if (!n) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
         if (n <= 0) n = 152;
+        cache[slot].store(n, std::memory_order_relaxed);
     }
     return n;
 }

@@ -751,15 +751,19 @@ extern "C" s2c_status s2c_dda_cluster_bitset(int64_t P, const int32_t* edge_ids,
     const size_t rs = raster_smem(g);
     S2C_REQUIRE(rs <= 200 * 1024, "dda_cluster_bitset: tile too large for shared memory");
     cudaStream_t st = (cudaStream_t)stream;
-    static size_t cfg_raster = 0;
-    static bool cfg_bin = false;
-    if (rs > cfg_raster) {
+    // kernel attributes and the raster's occupancy belong to a device: cached per device
+    static std::atomic<size_t> cfg_raster[kMaxDevices];
+    static std::atomic<bool> cfg_bin[kMaxDevices];
+    static std::atomic<int> occ_cache[kMaxDevices];
+    static std::atomic<size_t> occ_rs[kMaxDevices];
+    const int slot = current_device_slot();
+    if (rs > cfg_raster[slot].load()) {
         cudaFuncSetAttribute(dda_tile_raster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rs);
-        cfg_raster = rs;
+        cfg_raster[slot].store(rs);
     }
-    if (!cfg_bin) {
+    if (!cfg_bin[slot].load()) {
         cudaFuncSetAttribute(dda_bin_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bin_smem());
-        cfg_bin = true;
+        cfg_bin[slot].store(true);
     }
     const int T = g.num_tiles;
     fused_init<<<grid_for(std::max(T, (int)H_WORDS), 256, 2048), 256, 0, st>>>(w.hdr, w.nrec, w.nent, w.rfill, T);
@@ -774,12 +778,12 @@ extern "C" s2c_status s2c_dda_cluster_bitset(int64_t P, const int32_t* edge_ids,
         return s;
     scatter_records<<<2 * num_sms(), 256, 0, st>>>(w, T);
     S2C_CHECK_LAUNCH("scatter_records");
-    static int occ = 0;
-    static size_t occ_rs = 0;
-    if (occ_rs != rs) {
+    int occ = occ_cache[slot].load();
+    if (occ_rs[slot].load() != rs || occ < 1) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dda_tile_raster_kernel, kRasterThreads, rs);
-        occ_rs = rs;
         if (occ < 1) occ = 1;
+        occ_cache[slot].store(occ);
+        occ_rs[slot].store(rs);
     }
     const unsigned rgrid = (unsigned)std::min<int64_t>((int64_t)occ * num_sms(), T);
     dda_tile_raster_kernel<<<rgrid, kRasterThreads, rs, st>>>(g, w, bitset);
