@@ -38,3 +38,35 @@ def test_workspace_queries_are_pure_host(lib_built):
     assert L.s2c_dda_cluster_bitset_workspace_size(4_950_000, 1, 1024, 1024, 64) > 8 * 4_950_000
     assert L.s2c_dda_compute_span_workspace_size(1000) > 0
     assert L.s2c_filter_valid_fragments_workspace_size(0) > 0
+
+
+def test_argument_errors_come_back_as_status_without_a_gpu(lib_built):
+    """Invalid sizes and null pointers are rejected on the host before any CUDA call, with a
+    status code and a message (the library never exits the process)."""
+    import ctypes
+    from strns2cards_gb300 import _lib
+    L = _lib.lib()
+    t3 = (ctypes.c_float * 3)(0.0, 1.0, 0.0)
+    cases = [
+        ("s2c_strand_frames", (-1, 4, None, None, None, None, None, None, None, 3, None, None)),
+        ("s2c_strand_frames", (2, 4, None, None, None, None, None, None, None, 3, None, None)),   # null strands
+        ("s2c_wisp_frames", (3, None, 10, 1, None, t3, t3, t3, None, None, None, None)),          # V < 2
+        ("s2c_wisp_frames", (3, None, 10, 8, None, t3, t3, t3, None, None, None, None)),          # nulls
+        ("s2c_wisp_rotate", (2, None, 10, 0, None, None, None, None, None, None, None)),          # V = 0
+        ("s2c_align_strands", (10, L.s2c_align_strands_max_points() + 1, None, 1, None, None, None, t3, 0.05,
+                               None, None, None)),                                                # too long to stage
+        ("s2c_align_strands", (10, 1, None, 1, None, None, None, t3, 0.05, None, None, None)),    # V < 2
+        ("s2c_build_edges_device", (-1, None, 4, None, None, None, None, None, 0, None)),
+        ("s2c_build_edges_device", (5, None, 4, None, None, None, None, None, 0, None)),          # null counts
+        ("s2c_resample_strands_by_arclength_host", (2, None, None, 1, None)),                     # target < 2
+    ]
+    for name, args in cases:
+        st = getattr(L, name)(*args)
+        assert st == _lib.S2C_ERR_INVALID, (name, args, st)
+        assert L.s2c_last_error(), name
+    # empty problems are no-ops that succeed
+    assert L.s2c_strand_frames(0, 4, None, None, None, None, None, None, None, 3, None, None) == 0
+    assert L.s2c_wisp_frames(0, None, 0, 4, None, t3, t3, t3, None, None, None, None) == 0
+    assert L.s2c_align_strands(0, 8, None, 0, None, None, None, t3, 0.05, None, None, None) == 0
+    assert L.s2c_align_strands_max_points() >= 64
+    assert L.s2c_build_edges_device_workspace_size(0, 0) > 0
