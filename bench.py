@@ -409,6 +409,45 @@ def wl_antialias(list_path=False):
                          + how)
 
 
+def wl_antialias_2048():
+    """The differentiation case at full size: antialias backward of 4,096 cards (16 x 4
+    quads) of the 100,000 x 64 strand model against its strands' bitset, 2048x2048, K=4096
+    (two 2 GiB bitsets); the gradient w.r.t. the card vertices (scalar upstream gradient:
+    the loss has no image-gradient input)."""
+    import torch
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    H, K = 2048, 4096
+    strands, mvp, cards = _cards_scene(100_000, 64, 4096, 16, 4, H)
+    pos = syn.project(cards.verts, mvp)
+    spos = syn.project(strands.reshape(-1, 3), mvp)
+    sedges = syn.strand_edges(100_000, 64)
+    se2c = (np.arange(sedges.shape[0]) * K // sedges.shape[0]).astype(np.int32)
+    edges, e2t = s2c.build_edges_from_triangles(cards.tri)
+    e2c = cards.tri2cluster[e2t[:, 0]].astype(np.int32)
+    host = {"pos": pos, "tri": cards.tri, "edges": edges, "e2t": e2t, "e2c": e2c}
+    V, E = pos.shape[1], edges.shape[0]
+    S = K // 32
+
+    def setup(d):
+        dev = d["pos"].device
+        tgt = s2c.dda_cluster_bitset((H, H), torch.from_numpy(spos).to(dev), torch.from_numpy(sedges).to(dev),
+                                     torch.from_numpy(se2c).to(dev), K)
+        _, bits = s2c.rasterize_fused((H, H), d["pos"], d["tri"], torch.from_numpy(cards.tri2cluster).to(dev), K,
+                                      want_rast=False)
+        return {"tgt": tgt, "bits": bits}
+
+    def step(d, st):
+        return s2c.antialiased_cluster_bitset_grad(st["bits"], st["tgt"], d["pos"], d["tri"], d["edges"], d["e2t"],
+                                                   d["e2c"], 7.0, 0.5)
+    return dict(name="antialias_2048", host=host, setup=setup, step=step, units=E, unit="Medge/s", scale=1e6,
+                metric="card edges through the antialiased bitset-loss backward per second",
+                alg_bytes=2 * 4 * H * H * S + 16 * V + 20 * E + 16 * V, launches=None,
+                workload="antialias backward of 4,096 cards (16x4 quads, %d edges) of the 100,000x64 strand "
+                         "model against its strands' bitset, 2048x2048, K=4096: bitset planes + one fused pass "
+                         "per (view, edge)" % E)
+
+
 def wl_iteration():
     """One plain fit iteration of the 50,000 x 100 model: card raster (rast + bitset),
     antialias forward (XOR loss) and backward, per-card IoU."""
@@ -856,6 +895,7 @@ def wl_build_edges():
 
 WORKLOADS = {"msaa": wl_msaa, "resample": wl_resample, "tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
+             "antialias_2048": wl_antialias_2048,
              "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
              "laplacian": wl_laplacian, "align_wisps": wl_align_wisps, "build_edges": wl_build_edges}
