@@ -317,9 +317,21 @@ def antialiased_cluster_bitset_grad_planes(bitset_planes, target_planes, shape, 
     """The fused gradient from cluster planes (``bitset_to_planes``) of the bitset and the
     target; ``shape`` = (B, H, W, S) of the bitsets."""
     B, H, W, S = shape
-    V = pos.shape[1]
     _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(edges, _i32, 2, 2, "edges")
+    _arr(edge2tri, _i32, 2, 2, "edge2tri")
+    _arr(edge2cluster, _i32, 1, name="edge2cluster")
     _cuda(bitset_planes, target_planes, pos, tri, edges, edge2tri, edge2cluster)
+    pshape = (B, 32 * S, H, (W + 31) // 32)
+    for t, nm in ((bitset_planes, "bitset_planes"), (target_planes, "target_planes")):
+        if tuple(t.shape) != pshape or t.dtype != _i32 or not t.is_contiguous():
+            raise RuntimeError(f"antialiased_cluster_bitset_grad_planes: {nm} must be contiguous int32 {pshape}.")
+    if pos.shape[0] != B:
+        raise RuntimeError("antialiased_cluster_bitset_grad: bitset, target_bitset and pos views must match.")
+    if edge2tri.shape[0] != edges.shape[0] or edge2cluster.shape[0] < edges.shape[0]:
+        raise RuntimeError("antialiased_cluster_bitset_grad: edge2tri / edge2cluster must cover every edge.")
+    V = pos.shape[1]
     if d_pos is None:
         d_pos = torch.zeros_like(pos)
     need = _lib.lib().s2c_antialiased_cluster_bitset_grad_planes_workspace_size(B, V, edges.shape[0])

@@ -9,6 +9,8 @@ from __future__ import annotations
 
 from typing import Any, Tuple
 
+import weakref
+
 import torch
 
 from . import _core
@@ -55,6 +57,41 @@ class _AntialiasedClusterBitsetLossFn(torch.autograd.Function):
         return None, grad_output * d_pos, None
 
 
+class _TargetPlanesCache:
+    """Cluster planes of target bitsets.  A fitting loop passes the same target to the loss
+    every iteration (``3_fitting.py``), so its transpose is kept while that tensor object is
+    alive and unmodified: an entry holds a weak reference to the tensor and its version
+    counter and data pointer, and is used only when all three still match."""
+
+    def __init__(self, capacity: int = 4):
+        self.capacity = capacity
+        self._entries = []   # (weakref, version, data_ptr, planes)
+
+    def planes(self, target: torch.Tensor) -> torch.Tensor:
+        live = []
+        hit = None
+        for ref, ver, dp, pl in self._entries:
+            t = ref()
+            if t is None:
+                continue
+            live.append((ref, ver, dp, pl))
+            if t is target and ver == target._version and dp == target.data_ptr():
+                hit = pl
+        self._entries = live
+        if hit is not None:
+            return hit
+        pl = _core.bitset_to_planes(target)
+        self._entries.append((weakref.ref(target), target._version, target.data_ptr(), pl))
+        self._entries = self._entries[-self.capacity:]
+        return pl
+
+    def clear(self):
+        self._entries = []
+
+
+target_planes_cache = _TargetPlanesCache()
+
+
 def antialiased_cluster_bitset_grad(
     bitset: torch.Tensor,
     target_bitset: torch.Tensor,
@@ -82,9 +119,17 @@ def antialiased_cluster_bitset_grad(
                                                   target_bitset.contiguous(), pos.contiguous(), edges.contiguous(),
                                                   normals, edge2cluster.contiguous(), d_pos, kernel_radius, rho)
         return d_pos
-    return _core.antialiased_cluster_bitset_grad(bitset.contiguous(), target_bitset.contiguous(), pos.contiguous(),
-                                                 tri.contiguous(), edges.contiguous(), edge2tri.contiguous(),
-                                                 edge2cluster.contiguous(), kernel_radius, rho)
+    # the bitset's cluster planes each call, the target's from the cache (same result as
+    # the bitset entry point, which transposes both)
+    bits = bitset.contiguous()
+    if tuple(target_bitset.shape) != tuple(bits.shape) or target_bitset.dtype != bits.dtype:
+        raise RuntimeError("antialiased_cluster_bitset_grad: bitset, target_bitset and pos views must match.")
+    tplanes = target_planes_cache.planes(target_bitset if target_bitset.is_contiguous()
+                                         else target_bitset.contiguous())
+    return _core.antialiased_cluster_bitset_grad_planes(_core.bitset_to_planes(bits), tplanes, tuple(bits.shape),
+                                                        pos.contiguous(), tri.contiguous(), edges.contiguous(),
+                                                        edge2tri.contiguous(), edge2cluster.contiguous(),
+                                                        kernel_radius, rho)
 
 
 def antialiased_cluster_bitset_loss(

@@ -177,3 +177,32 @@ def test_bitset_to_planes(shape):
     pad[..., :W] = bits
     ref = (pad.reshape(B, 32 * S, H, WQ, 32) << np.arange(32, dtype=np.uint32)).sum(-1, dtype=np.uint64).astype(np.uint32)
     assert np.array_equal(got, ref)
+
+
+def test_target_planes_cache_is_exact_and_follows_writes():
+    # the drop-in gradient keeps the target's cluster planes while the target tensor is
+    # alive and unmodified: the result equals the bitset entry point (which transposes both
+    # bitsets every call) bit for bit, and an in-place write to the target is seen
+    import gc
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    from strns2cards_gb300.antialias import target_planes_cache
+    a = golden("antialias.npz")
+    bits, tgt, pos, tri, edges, e2t, e2c = (cu(a[k]) for k in ("bitset", "target", "pos", "tri", "edges", "edge2tri",
+                                                                 "edge2cluster"))
+    target_planes_cache.clear()
+    ref = _core.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    g1 = s2c.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    g2 = s2c.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)   # cached planes
+    assert torch.equal(g1, ref) and torch.equal(g2, ref)
+    tgt.bitwise_xor_(bits)                       # in place: the version counter moves on
+    ref2 = _core.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    g3 = s2c.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    assert torch.equal(g3, ref2) and not torch.equal(ref2, ref)
+    # a dead target leaves no entry behind
+    del tgt
+    gc.collect()
+    target_planes_cache.planes(bits)
+    assert len(target_planes_cache._entries) == 1
+    with pytest.raises(RuntimeError):
+        s2c.antialiased_cluster_bitset_grad(bits, bits[:, :, :-1].contiguous(), pos, tri, edges, e2t, e2c, 7.0, 0.5)
