@@ -354,7 +354,7 @@ S2C_API s2c_status s2c_strand_frames(int N, int V, const float* strands, const f
 /* replaces: the per-wisp loop of align_wisps (curve_utils.py:521-568): one CTA per wisp.
  * Wisp w holds strands offsets[w] .. offsets[w+1]-1 of strands (num_strands, V, 3), V >= 2.
  * centre[w] = mean root; longest[w] = the strand of greatest polyline length (first on
- * ties); the least-variance axis of the centred roots (FP64 second moment and a Jacobi
+ * ties); the least-variance axis of the centred roots (FP32 second moment and a Jacobi
  * eigen-solve, in place of the host SVD; identity axes below 3 strands) and the longest
  * strand's view and down directions give the source frame; R_global[w] (3x3 row-major) =
  * [t_dst n_dst b_dst][T_src N_src B_src]^T.  An empty or out-of-range wisp gets the

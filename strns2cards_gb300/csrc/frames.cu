@@ -1,14 +1,22 @@
-// Strand frames and wisp alignment (the reference's curve_utils.py:9-165 and 250-296:
+// Strand frames and wisp alignment (the reference's curve_utils.py:9-165 and 243-308:
 // minimal_rotation, tangent_frame, compute_bishop_frame, compute_aligned_strands,
-// compute_alignment_rotation; and the per-wisp frame of align_wisps, :481-570).
+// compute_alignment_rotation; and align_wisps, :481-607).
 //
 // The reference runs the Bishop (rotation-minimising) frame recurrence as a Python loop
 // over the points of all strands and the wisp frames as a Python loop over wisps with a
-// host SVD each.  Here one thread walks one strand's recurrence and writes its frames, its
-// alignment rotations and its canonical handle in the same pass; one CTA per wisp reduces
-// its roots (centre, 3x3 second moment in FP64, a cyclic Jacobi eigen-solve in place of the
-// SVD: the least-variance axis is the singular vector the frame uses) and builds the
-// wisp's rotation.  FP32 elsewhere, with the reference's formulas.
+// host SVD each.  Here:
+//   strand_frames_kernel  one warp per strand, one lane per point: the recurrence as a warp
+//                         scan of 3x3 maps (frame_chunk), frames, alignment rotations and
+//                         canonical handles in one pass;
+//   wisp_frames_kernel    one CTA per wisp: root centre, longest strand, FP32 second moment
+//                         of the centred roots and a cyclic Jacobi eigen-solve in place of
+//                         the SVD (the least-variance axis is the singular vector the frame
+//                         uses), the wisp's rotation;
+//   wisp_rotate_kernel    the strands and handles turned into their wisp's frame;
+//   align_strands_kernel  smoothing, rotation, frames and skinning of each strand fused
+//                         (one warp per strand staged in shared memory), with the same
+//                         device code as the separate steps.
+// FP32 throughout, with the reference's formulas.
 #include <algorithm>
 
 #include "common.cuh"
