@@ -72,7 +72,8 @@ def load_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 20 ms during the timed region; the
+    sampler has written its first sample before the region starts (it takes ~0.1 s to start)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -88,8 +89,13 @@ class ClockSampler:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            t0 = time.perf_counter()
+            while time.perf_counter() - t0 < 3.0 and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
+            # samples taken before the region are dropped in summary()
+            self.skip = sum(1 for _ in open(self.path))
         except Exception:
             self.proc = None
         return self
@@ -106,7 +112,11 @@ class ClockSampler:
         if not self.path or not os.path.exists(self.path):
             return None
         rows = []
-        for line in open(self.path):
+        lines = open(self.path).readlines()
+        # keep the pre-region sample(s) only when the region itself produced none
+        if len(lines) > getattr(self, "skip", 0):
+            lines = lines[getattr(self, "skip", 0):]
+        for line in lines:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -971,7 +981,7 @@ def run_workload(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
