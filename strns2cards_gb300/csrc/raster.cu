@@ -210,13 +210,10 @@ struct FusedRaster {
     const int64_t* __restrict__ total;      // device: sum of the areas
 };
 
-__device__ __forceinline__ void raster_pixel(const FusedRaster& F, const float* px_lut, const float* py_lut, int ob,
-                                             int ot, int x, int y) {
+// one pixel of a triangle whose corners are loaded
+__device__ __forceinline__ void raster_covered(const FusedRaster& F, const float* px_lut, const float* py_lut, int ob,
+                                               int ot, float4 P0, float4 P1, float4 P2, int x, int y) {
     if (x < 0 || x >= F.W || y < 0 || y >= F.H) return;
-    const int i0 = __ldg(F.R.tri + 3 * ot), i1 = __ldg(F.R.tri + 3 * ot + 1), i2 = __ldg(F.R.tri + 3 * ot + 2);
-    if ((unsigned)i0 >= (unsigned)F.R.V || (unsigned)i1 >= (unsigned)F.R.V || (unsigned)i2 >= (unsigned)F.R.V) return;
-    const float4* pb = F.R.pos4 + (int64_t)ob * F.R.V;
-    const float4 P0 = __ldg(pb + i0), P1 = __ldg(pb + i1), P2 = __ldg(pb + i2);
     const float px = px_lut ? px_lut[x] : ndc_of(x, (float)F.W);
     const float py = py_lut ? py_lut[y] : ndc_of(y, (float)F.H);
     const TriEdges e = tri_edges(P0, P1, P2, px, py);
@@ -236,6 +233,27 @@ __device__ __forceinline__ void raster_pixel(const FusedRaster& F, const float* 
                 atomicOr(F.planes + (((int64_t)ob * 32 * F.S + c) * F.H + y) * F.WQ + (x >> 5), 1u << (x & 31));
         }
     }
+}
+
+// the corners of triangle ot of view ob; false for an out-of-range vertex index
+__device__ __forceinline__ bool raster_corners(const FusedRaster& F, int ob, int ot, float4& P0, float4& P1,
+                                               float4& P2) {
+    const int i0 = __ldg(F.R.tri + 3 * ot), i1 = __ldg(F.R.tri + 3 * ot + 1), i2 = __ldg(F.R.tri + 3 * ot + 2);
+    if ((unsigned)i0 >= (unsigned)F.R.V || (unsigned)i1 >= (unsigned)F.R.V || (unsigned)i2 >= (unsigned)F.R.V)
+        return false;
+    const float4* pb = F.R.pos4 + (int64_t)ob * F.R.V;
+    P0 = __ldg(pb + i0);
+    P1 = __ldg(pb + i1);
+    P2 = __ldg(pb + i2);
+    return true;
+}
+
+__device__ __forceinline__ void raster_pixel(const FusedRaster& F, const float* px_lut, const float* py_lut, int ob,
+                                             int ot, int x, int y) {
+    if (x < 0 || x >= F.W || y < 0 || y >= F.H) return;
+    float4 P0, P1, P2;
+    if (!raster_corners(F, ob, ot, P0, P1, P2)) return;
+    raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x, y);
 }
 
 // local / w for 0 <= local, 1 <= w: float estimate corrected by one step (exact while
@@ -330,14 +348,23 @@ __global__ void __launch_bounds__(256, 5) tri_fused_kernel(FusedRaster F) {
             }
             const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
             if (j < end) {
+                // work unit j: a pair of horizontally adjacent bounding-box pixels (the
+                // triangle's corners are loaded once for both)
                 const int64_t o = t0 + ow;
                 const int ob = (int)F.R.divT.div((uint32_t)o);
                 const int ot = (int)o - ob * F.R.T;
                 const int4 rc = F.rects[o];
                 const int local = (int)(j - (ow > 0 ? prev : start));
+                const int wp = (rc.w + 1) >> 1;
                 int r;
-                const int q = divmod_small(local, rc.w, r);
-                raster_pixel(F, px_lut, py_lut, ob, ot, rc.z + r, rc.x + q);
+                const int q = divmod_small(local, wp, r);
+                const int x = rc.z + 2 * r, y = rc.x + q;
+                float4 P0, P1, P2;
+                // only the bounding box's own pixels, as the list path tests
+                if (q < rc.y && y >= 0 && y < F.H && raster_corners(F, ob, ot, P0, P1, P2)) {
+                    raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x, y);
+                    if (2 * r + 1 < rc.w) raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x + 1, y);
+                }
             }
             base = end;
         }
@@ -354,7 +381,8 @@ __global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B,
         const int t = (int)idx - b * R.T;
         const int4 rc = tri_rect(H, W, R, b, t);
         rects[idx] = rc;
-        areas[idx] = (int32_t)((uint32_t)rc.y * (uint32_t)rc.w);
+        // work units of the balanced raster: pairs of horizontally adjacent pixels per row
+        areas[idx] = (int32_t)((uint32_t)rc.y * (((uint32_t)rc.w + 1u) >> 1));
     }
 }
 
