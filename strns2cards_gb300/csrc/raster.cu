@@ -277,7 +277,7 @@ constexpr int kRasterChunk = 1024;
 // Balanced pass: warps take equal chunks of the global bbox-pixel index space.  A warp
 // keeps a window of 32 consecutive triangles' prefix values in its lanes, slides it along
 // the chunk, and each lane finds the owner of its pixel with a 5-step shuffle search.
-__global__ void __launch_bounds__(256, 5) tri_fused_kernel(FusedRaster F) {
+__global__ void __launch_bounds__(256, 4) tri_fused_kernel(FusedRaster F) {
     extern __shared__ float lut[];
     const bool use_lut = F.W + F.H <= 8192;
     if (use_lut) {
