@@ -458,6 +458,130 @@ def wl_antialias_2048():
                          "per (view, edge)" % E)
 
 
+def _dda_scene_full():
+    from strns2cards_gb300 import synthetic as syn
+    sc = syn.strand_scene(NUM_STRANDS, NUM_VERTS, per_cluster=PER_CLUSTER, num_views=1, seed=0)
+    return sc
+
+
+def wl_dda_list():
+    """The reference's op sequence for the strands' bitset (dda_compute_fragments, then
+    cluster_mask_from_fragments), 50,000 x 100 strands, 1024x1024, K=2048."""
+    import strns2cards_gb300 as s2c
+    sc = _dda_scene_full()
+    host = {"pos": sc.pos, "edges": sc.edges, "e2c": sc.edge2cluster}
+    H = 1024
+
+    def step(d, st):
+        fp, fa = s2c.dda_compute_fragments((H, H), d["pos"], d["edges"])
+        return s2c.cluster_mask_from_fragments((H, H), fp, fa, d["e2c"], 2048)
+    E, V = sc.edges.shape[0], sc.pos.shape[1]
+    return dict(name="dda_list", host=host, step=step, units=E, unit="Gseg/s", scale=1e9, dtype="i32",
+                metric="Gseg/s DDA+bitset through the reference's op sequence (fragment list)",
+                alg_bytes=16 * V + 12 * E + 4 * H * H * 64, launches=None,
+                workload="dda_compute_fragments + cluster_mask_from_fragments of 50,000x100 strands (4.95M "
+                         "segments), 1024x1024, K=2048: fragment list, order-preserving compaction, bit OR")
+
+
+def _rast_scene_full():
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    _, mvp, cards = _cards_scene(50_000, 100, 2048, 16, 4, 1024)
+    pos = syn.project(cards.verts, mvp)
+    return pos, cards
+
+
+def wl_interpolate():
+    """Attribute interpolation forward + backward (upstream image gradient N(0,1), seed 0) over
+    the rast of the 2,048 cards, 1024x1024, 3 channels."""
+    import torch
+    import strns2cards_gb300 as s2c
+    pos, cards = _rast_scene_full()
+    V, H, C = pos.shape[1], 1024, 3
+    attr = np.random.default_rng(0).normal(size=(V, C)).astype(np.float32)
+    grad = torch.randn((1, H, H, C), generator=torch.Generator().manual_seed(0)).numpy()
+    host = {"pos": pos, "tri": cards.tri, "attr": attr, "grad": grad}
+
+    def setup(d):
+        return {"rast": s2c.rasterize((H, H), d["pos"], d["tri"])}
+
+    def step(d, st):
+        a = d["attr"].detach().requires_grad_(True)
+        img = s2c.interpolate_triangle_attributes(st["rast"], a, d["tri"])
+        img.backward(d["grad"])
+        return img, a.grad
+    return dict(name="interpolate", host=host, setup=setup, step=step, units=H * H, unit="Mpix/s", scale=1e6,
+                metric="pixels interpolated forward and backward per second (3 channels)",
+                alg_bytes=2 * 16 * H * H + 4 * C * H * H * 2 + 12 * 2 * V * C, launches=None,
+                workload="interpolate_triangle_attributes fwd + bwd (N(0,1) image gradient) of 3 channels over the "
+                         "rast of 2,048 cards, 1024x1024")
+
+
+def wl_dda_interpolate():
+    """Line-attribute interpolation forward + backward over the strands' DDA rast (the
+    fragment list's depth-resolved raster), 1024x1024, 3 channels."""
+    import torch
+    import strns2cards_gb300 as s2c
+    sc = _dda_scene_full()
+    V, H, C = sc.pos.shape[1], 1024, 3
+    attr = np.random.default_rng(0).normal(size=(V, C)).astype(np.float32)
+    grad = torch.randn((1, H, H, C), generator=torch.Generator().manual_seed(0)).numpy()
+    host = {"pos": sc.pos, "edges": sc.edges, "attr": attr, "grad": grad}
+
+    def setup(d):
+        fp, fa = s2c.dda_compute_fragments((H, H), d["pos"], d["edges"])
+        return {"rast": s2c.depth_test(1, (H, H), fp, fa)}
+
+    def step(d, st):
+        a = d["attr"].detach().requires_grad_(True)
+        img = s2c.dda_interpolate_attributes(st["rast"], a, d["edges"])
+        img.backward(d["grad"])
+        return img, a.grad
+    return dict(name="dda_interpolate", host=host, setup=setup, step=step, units=H * H, unit="Mpix/s", scale=1e6,
+                metric="pixels interpolated forward and backward per second (3 channels, line raster)",
+                alg_bytes=2 * 16 * H * H + 4 * C * H * H * 2 + 12 * 2 * V * C, launches=None,
+                workload="dda_interpolate_attributes fwd + bwd (N(0,1) image gradient) of 3 channels over the "
+                         "depth-resolved DDA raster of 50,000x100 strands, 1024x1024")
+
+
+def wl_bary_derivatives():
+    """Barycentric derivatives d(b0, b1)/d(x, y) of the 2,048 cards' rast, 1024x1024."""
+    import strns2cards_gb300 as s2c
+    pos, cards = _rast_scene_full()
+    H = 1024
+    host = {"pos": pos, "tri": cards.tri}
+
+    def setup(d):
+        return {"rast": s2c.rasterize((H, H), d["pos"], d["tri"])}
+
+    def step(d, st):
+        return s2c.barycentric_derivatives(st["rast"], d["pos"], d["tri"])
+    return dict(name="bary_derivatives", host=host, setup=setup, step=step, units=H * H, unit="Mpix/s", scale=1e6,
+                metric="pixels of barycentric derivatives per second",
+                alg_bytes=16 * H * H + 16 * H * H, launches=1,
+                workload="barycentric_derivatives (rast + the triangles' clip corners -> d(b0,b1)/d(x,y)) of the "
+                         "2,048 cards' rast, 1024x1024")
+
+
+def wl_bitset_stats():
+    """popcount_bitset and accumulate_bitset_rgb of the strands' cluster bitset (1024x1024, K=2048)."""
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(0)
+    H, S = 1024, 64
+    bits = rng.integers(0, 2 ** 31 - 1, size=(1, H, H, S), dtype=np.int64).astype(np.int32)
+    bits &= (rng.random(bits.shape) < 0.05).astype(np.int32) * -1   # sparse, as hair bitsets are
+    rgb = rng.random((32 * S, 3), dtype=np.float32)
+    host = {"bits": bits, "rgb": rgb}
+
+    def step(d, st):
+        return s2c.popcount_bitset(d["bits"]), s2c.accumulate_bitset_rgb(d["bits"], d["rgb"])
+    return dict(name="bitset_stats", host=host, step=step, units=2 * 4 * H * H * S, unit="GB/s", scale=1e9,
+                metric="bitset bytes read per second (popcount + colour accumulation)",
+                alg_bytes=2 * 4 * H * H * S + 4 * H * H + 12 * H * H, launches=2,
+                workload="popcount_bitset + accumulate_bitset_rgb of an int32 bitset (1, 1024, 1024, 64), K=2048, "
+                         "5 % of the words non-zero")
+
+
 def wl_iteration():
     """One plain fit iteration of the 50,000 x 100 model: card raster (rast + bitset),
     antialias forward (XOR loss) and backward, per-card IoU."""
@@ -905,7 +1029,9 @@ def wl_build_edges():
 
 WORKLOADS = {"msaa": wl_msaa, "resample": wl_resample, "tri_raster": wl_tri_raster, "tri_raster_list": lambda: wl_tri_raster(True),
              "antialias": wl_antialias, "antialias_list": lambda: wl_antialias(True), "iteration": wl_iteration,
-             "antialias_2048": wl_antialias_2048,
+             "antialias_2048": wl_antialias_2048, "dda_list": wl_dda_list, "interpolate": wl_interpolate,
+             "dda_interpolate": wl_dda_interpolate, "bary_derivatives": wl_bary_derivatives,
+             "bitset_stats": wl_bitset_stats,
              "cluster_iou": wl_cluster_iou,
              "smooth_strands": wl_smooth_strands, "skinning": wl_skinning, "lbs": wl_lbs,
              "laplacian": wl_laplacian, "align_wisps": wl_align_wisps, "build_edges": wl_build_edges}
