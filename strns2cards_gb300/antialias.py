@@ -65,23 +65,26 @@ class _TargetPlanesCache:
 
     def __init__(self, capacity: int = 4):
         self.capacity = capacity
-        self._entries = []   # (weakref, version, data_ptr, planes)
+        self._entries = []   # (weakref, version, data_ptr, planes, stream that wrote them)
 
     def planes(self, target: torch.Tensor) -> torch.Tensor:
         live = []
         hit = None
-        for ref, ver, dp, pl in self._entries:
+        for ref, ver, dp, pl, st in self._entries:
             t = ref()
             if t is None:
                 continue
-            live.append((ref, ver, dp, pl))
+            live.append((ref, ver, dp, pl, st))
             if t is target and ver == target._version and dp == target.data_ptr():
-                hit = pl
+                hit = (pl, st)
         self._entries = live
+        cur = torch.cuda.current_stream(target.device)
         if hit is not None:
-            return hit
+            if hit[1] != cur:
+                cur.wait_stream(hit[1])   # planes written on another stream
+            return hit[0]
         pl = _core.bitset_to_planes(target)
-        self._entries.append((weakref.ref(target), target._version, target.data_ptr(), pl))
+        self._entries.append((weakref.ref(target), target._version, target.data_ptr(), pl, cur))
         self._entries = self._entries[-self.capacity:]
         return pl
 
