@@ -15,7 +15,8 @@
 //           (hash of tile ids, warp-aggregated counters), written contiguously per tile,
 //           and one (tile, start, count) record per touched tile goes to a record pool.
 //  scan     exclusive offsets of the per-tile record counts.
-//  scatter  records sorted by tile; tiles with many entries listed first.
+//  scatter  records sorted by tile (each carries its rank in the tile from the bin pass);
+//           tiles with many entries listed first.
 //  raster   persistent CTAs take tiles from a queue (heavy ones first): clear a
 //           shared-memory copy of the tile's bitset, replay its entries with
 //           shared-memory atomicOr, write the whole tile (zeros included) once with
@@ -23,6 +24,7 @@
 //  fixup    chunks whose entries did not fit (chunk buffer, hash table, entry or record
 //           pool) are rasterised with global atomicOr on top of the finished bitset.
 #include <algorithm>
+#include <climits>
 
 #include "lines.cuh"
 #include "scan.cuh"
@@ -39,7 +41,7 @@ constexpr int kRasterThreads = 512;
 constexpr int kMaxRun = 28;                    // fragments per entry (27 step bits)
 constexpr int kHeavy = 8192;                   // entries that make a tile "heavy"
 
-enum { H_ENT = 0, H_REC = 1, H_OVER = 2, H_BAD = 3, H_WORK = 4, H_HEAVY = 5, H_WORDS = 16 };
+enum { H_ENT = 0, H_REC = 1, H_OVER = 2, H_WORK = 4, H_HEAVY = 5, H_WORDS = 16 };
 
 struct Geo {
     int B, H, W, S;
@@ -52,11 +54,10 @@ struct Ws {
     long long* hdr;
     int32_t* nrec;      // records per tile
     int32_t* nent;      // entries per tile
-    int32_t* rfill;     // scatter cursors
     int32_t* roff;      // exclusive record offsets (inclusive scan, then shifted on use)
     int32_t* heavy;     // heavy tile list
     int32_t* over;      // overflowed chunk ids
-    int4* recs;         // (tile, start, count, -)
+    int4* recs;         // (tile, start, count, rank among the tile's records)
     int2* sorted;       // (start, count) grouped by tile
     uint2* entries;
     void* scan_ws;      // scan scratch
@@ -87,7 +88,6 @@ static size_t layout(void* base, size_t bytes, int64_t P, const Geo& g, Ws& w) {
     w.hdr = c.take<long long>(H_WORDS);
     w.nrec = c.take<int32_t>(T);
     w.nent = c.take<int32_t>(T);
-    w.rfill = c.take<int32_t>(T);
     w.roff = c.take<int32_t>(T);
     w.heavy = c.take<int32_t>(T);
     w.chunk_cap = std::max<int64_t>((P + kChunk - 1) / kChunk, 1);
@@ -103,13 +103,12 @@ static size_t layout(void* base, size_t bytes, int64_t P, const Geo& g, Ws& w) {
     return fixed;
 }
 
-__global__ void fused_init(long long* hdr, int32_t* nrec, int32_t* nent, int32_t* rfill, int T) {
+__global__ void fused_init(long long* hdr, int32_t* nrec, int32_t* nent, int T) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < H_WORDS) hdr[i] = 0;
     for (int t = i; t < T; t += gridDim.x * blockDim.x) {
         nrec[t] = 0;
         nent[t] = 0;
-        rfill[t] = 0;
     }
 }
 
@@ -127,19 +126,13 @@ __device__ __forceinline__ int ht_slot(int* keys, int key) {
     return -1;
 }
 
-// cluster of edge e; the reference carries the prim id as float(e + 1)
-__device__ __forceinline__ int cluster_of(const int32_t* __restrict__ p2c, int e, int E, int S, long long* bad) {
+// cluster of edge e, -1 where the id or the cluster is out of range (the primitive is
+// skipped); the reference carries the prim id as float(e + 1)
+__device__ __forceinline__ int cluster_of(const int32_t* __restrict__ p2c, int e, int E, int S) {
     const int pr = prim_roundtrip(e);
-    if (pr < 0 || pr >= E) {
-        atomicAdd((unsigned long long*)bad, 1ull);
-        return -1;
-    }
+    if (pr < 0 || pr >= E) return -1;
     const int c = __ldg(p2c + pr);
-    if (c < 0 || c >= 32 * S) {
-        atomicAdd((unsigned long long*)bad, 1ull);
-        return -1;
-    }
-    return c;
+    return c >= 0 && c < 32 * S ? c : -1;
 }
 
 // Depth test skipped when both ends are finite, 1e-30 <= w <= 1e30 and |z| <= 0.999 w:
@@ -153,16 +146,27 @@ __device__ __forceinline__ bool depth_always_passes(float4 a, float4 b) {
     return ok(a) && ok(b);
 }
 
+// A primitive with its cluster entry, loaded together one primitive ahead of its sweep;
+// craw = p2c[prim_roundtrip(e)], or INT_MIN where that id is outside [0, E).
 struct Lane {
     bool valid;
+    int craw;
     Prim q;
 };
 
-__device__ __forceinline__ Lane fetch(int64_t p, int64_t P, const Lines& L) {
+__device__ __forceinline__ Lane fetch(int64_t p, int64_t P, const Lines& L, const int32_t* __restrict__ p2c) {
     Lane l;
     l.valid = p < P && load_prim(p, L, l.q);
+    l.craw = INT_MIN;
+    if (l.valid) {
+        const int pr = prim_roundtrip(l.q.e);
+        if (pr >= 0 && pr < L.E) l.craw = __ldg(p2c + pr);
+    }
     return l;
 }
+
+// cluster_of on a prefetched entry
+__device__ __forceinline__ int cluster_checked(int craw, int S) { return craw >= 0 && craw < 32 * S ? craw : -1; }
 
 __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L, Geo g, const int32_t* __restrict__ p2c,
                                                               Ws w) {
@@ -220,14 +224,14 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
         }
     };
 
-    Lane cur = fetch(chunk0 + threadIdx.x, P, L);
+    Lane cur = fetch(chunk0 + threadIdx.x, P, L, p2c);
     for (int j = 0; j < kBinPPT; ++j) {
         Lane nxt;  // prefetch the next primitive of this thread
         nxt.valid = false;
-        if (j + 1 < kBinPPT) nxt = fetch(chunk0 + (int64_t)(j + 1) * kBinThreads + threadIdx.x, P, L);
+        if (j + 1 < kBinPPT) nxt = fetch(chunk0 + (int64_t)(j + 1) * kBinThreads + threadIdx.x, P, L, p2c);
         if (cur.valid) {
             const Span s = dda_span(cur.q.p0, cur.q.p1, g.H, g.W);
-            const int c = s.count > 0 ? cluster_of(p2c, cur.q.e, L.E, g.S, w.hdr + H_BAD) : -1;
+            const int c = s.count > 0 ? cluster_checked(cur.craw, g.S) : -1;
             if (c >= 0) {
                 const bool zfast = depth_always_passes(cur.q.p0, cur.q.p1);
                 const int axis = s.axis != 0.f;
@@ -448,8 +452,9 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
     for (int j = 0; j < 4; ++j) {
         if (!used[j]) continue;
         const int tile = ht_key[threadIdx.x * 4 + j];
-        w.recs[s_rbase + rrank[j]] = make_int4(tile, (int)(base + ebase[j]), v[j], 0);
-        atomicAdd(w.nrec + tile, 1);
+        // the count before this record is its rank among the tile's records
+        const int rank = atomicAdd(w.nrec + tile, 1);
+        w.recs[s_rbase + rrank[j]] = make_int4(tile, (int)(base + ebase[j]), v[j], rank);
         atomicAdd(w.nent + tile, v[j]);
     }
 }
@@ -462,7 +467,7 @@ __global__ void __launch_bounds__(256) scatter_records(Ws w, int T) {
     for (int64_t r = i0; r < nr; r += stride) {
         const int4 rc = w.recs[r];
         if (rc.x < 0 || rc.x >= T) continue;  // slot of a chunk that overflowed
-        const int pos = w.roff[rc.x] - w.nrec[rc.x] + atomicAdd(w.rfill + rc.x, 1);
+        const int pos = w.roff[rc.x] - w.nrec[rc.x] + rc.w;
         w.sorted[pos] = make_int2(rc.y, rc.z);
     }
     for (int64_t t = i0; t < T; t += stride)
@@ -703,7 +708,7 @@ __global__ void __launch_bounds__(256) dda_fixup_kernel(int64_t P, Lines L, Geo 
         Prim q;
         if (p >= P || !load_prim(p, L, q)) continue;
         const Span s = dda_span(q.p0, q.p1, g.H, g.W);
-        const int c = cluster_of(p2c, q.e, L.E, g.S, w.hdr + H_BAD);
+        const int c = cluster_of(p2c, q.e, L.E, g.S);
         if (c < 0) continue;
         for (int k = 0; k < s.count; ++k) {
             float x, y;
@@ -766,7 +771,7 @@ extern "C" s2c_status s2c_dda_cluster_bitset(int64_t P, const int32_t* edge_ids,
         cfg_bin[slot].store(true);
     }
     const int T = g.num_tiles;
-    fused_init<<<grid_for(std::max(T, (int)H_WORDS), 256, 2048), 256, 0, st>>>(w.hdr, w.nrec, w.nent, w.rfill, T);
+    fused_init<<<grid_for(std::max(T, (int)H_WORDS), 256, 2048), 256, 0, st>>>(w.hdr, w.nrec, w.nent, T);
     S2C_CHECK_LAUNCH("fused_init");
     const Lines L = make_lines(edge_ids, B, V, pos, E, edges);
     if (P > 0) {

@@ -5,7 +5,8 @@
 // compact_utils.cu:7-77), whose output order depends on block scheduling.  Here the
 // order is the input order, and nothing synchronises with the host unless the caller
 // asks for the count.  Reduce-then-scan in three launches: per-tile totals, a scan of
-// the tile totals in one CTA, then a per-tile scan that adds the tile offset.
+// the tile totals in one CTA, then a per-tile scan that adds the tile offset; an int32
+// scan of at most 16,384 values runs in one CTA and one launch.
 #include <cstdarg>
 #include <cstdio>
 
@@ -92,6 +93,35 @@ __global__ void __launch_bounds__(1024) scan_totals(int64_t* sums, int64_t ntile
     if (threadIdx.x == 0) *total = carry;
 }
 
+// The whole inclusive int32 prefix of n <= kSmallScanMax values in one CTA (one launch
+// instead of three); each thread owns up to kSmallScanItems consecutive values, so it
+// writes only what it read and in == out works.
+constexpr int kSmallScanThreads = 1024;
+constexpr int kSmallScanItems = 16;
+constexpr int64_t kSmallScanMax = (int64_t)kSmallScanThreads * kSmallScanItems;
+
+__global__ void __launch_bounds__(kSmallScanThreads) scan_small_i32(const int32_t* in, int n, int32_t* out,
+                                                                    int64_t* total) {
+    __shared__ int64_t wb[33];
+    const int per = (n + kSmallScanThreads - 1) / kSmallScanThreads;
+    const int i0 = threadIdx.x * per;
+    int32_t v[kSmallScanItems];
+    int64_t s = 0;
+#pragma unroll
+    for (int j = 0; j < kSmallScanItems; ++j) {
+        v[j] = (j < per && i0 + j < n) ? in[i0 + j] : 0;
+        s += v[j];
+    }
+    int64_t tot;
+    int64_t run = block_exclusive<int64_t>(s, wb, tot);
+#pragma unroll
+    for (int j = 0; j < kSmallScanItems; ++j) {
+        run += v[j];
+        if (j < per && i0 + j < n) out[i0 + j] = (int32_t)(uint32_t)(uint64_t)run;
+    }
+    if (threadIdx.x == 0) *total = tot;
+}
+
 // inclusive int32 prefix (wrapping like the reference's int scan)
 __global__ void __launch_bounds__(kScanThreads) tile_scan_i32(const int32_t* in, int64_t n,
                                                               const int64_t* offs, int32_t* out) {
@@ -158,6 +188,11 @@ s2c_status inclusive_scan_i32(const int32_t* in, int64_t n, int32_t* out, void* 
     if (n == 0) {
         cudaMemsetAsync(d_total, 0, sizeof(int64_t), st);
         return cuda_status(cudaGetLastError(), "scan: memset");
+    }
+    if (n <= kSmallScanMax) {
+        scan_small_i32<<<1, kSmallScanThreads, 0, st>>>(in, (int)n, out, d_total);
+        S2C_CHECK_LAUNCH("inclusive_scan_i32");
+        return S2C_OK;
     }
     tile_totals<<<(unsigned)nt, kScanThreads, 0, st>>>(CountI32{in}, n, sums);
     scan_totals<<<1, 1024, 0, st>>>(sums, nt, d_total);
