@@ -17,10 +17,10 @@
 //  scan     exclusive offsets of the per-tile record counts.
 //  scatter  records sorted by tile (each carries its rank in the tile from the bin pass);
 //           tiles with many entries listed first.
-//  raster   persistent CTAs take tiles from a queue (heavy ones first): clear a
-//           shared-memory copy of the tile's bitset, replay its entries with
-//           shared-memory atomicOr, write the whole tile (zeros included) once with
-//           coalesced 16-byte streaming stores.
+//  raster   persistent CTAs (3 per SM) take tiles from a queue (heavy ones first):
+//           replay the tile's entries into a shared-memory copy of its bitset with
+//           atomicOr (a run never leaves its tile, so it walks one shared index), write
+//           the whole tile (zeros included) once with coalesced 16-byte streaming stores.
 //  fixup    chunks whose entries did not fit (chunk buffer, hash table, entry or record
 //           pool) are rasterised with global atomicOr on top of the finished bitset.
 #include <algorithm>
@@ -146,20 +146,52 @@ __device__ __forceinline__ bool depth_always_passes(float4 a, float4 b) {
     return ok(a) && ok(b);
 }
 
-// A primitive with its cluster entry, loaded together one primitive ahead of its sweep;
-// craw = p2c[prim_roundtrip(e)], or INT_MIN where that id is outside [0, E).
+// A primitive with its cluster entry; craw = p2c[prim_roundtrip(e)], or INT_MIN where that
+// id is outside [0, E).
 struct Lane {
     bool valid;
     int craw;
     Prim q;
 };
 
-__device__ __forceinline__ Lane fetch(int64_t p, int64_t P, const Lines& L, const int32_t* __restrict__ p2c) {
+// Two-stage prefetch (the checks of load_prim, split): the edge (vertex pair) two primitives
+// ahead, then its positions and cluster entry one primitive ahead, so that no load waits on
+// another inside an iteration.
+struct PreEdge {
+    bool valid;
+    int b, e;
+    int2 ev;
+};
+
+__device__ __forceinline__ PreEdge fetch_edge(int64_t p, int64_t P, const Lines& L) {
+    PreEdge r;
+    r.valid = false;
+    r.b = 0;
+    r.e = 0;
+    r.ev = make_int2(0, 0);
+    if (p < P) {
+        const int64_t eid = L.edge_ids ? (int64_t)__ldg(L.edge_ids + p) : p;
+        if (eid >= 0 && eid < L.BE) {
+            r.b = L.BE == L.E ? 0 : (int)L.divE.div((uint32_t)eid);
+            r.e = (int)eid - r.b * L.E;
+            r.ev = __ldg(L.edges2 + r.e);
+            r.valid = true;
+        }
+    }
+    return r;
+}
+
+__device__ __forceinline__ Lane fetch_pos(const PreEdge& r, const Lines& L, const int32_t* __restrict__ p2c) {
     Lane l;
-    l.valid = p < P && load_prim(p, L, l.q);
+    l.valid = r.valid && (unsigned)r.ev.x < (unsigned)L.V && (unsigned)r.ev.y < (unsigned)L.V;
+    l.q.b = r.b;
+    l.q.e = r.e;
     l.craw = INT_MIN;
     if (l.valid) {
-        const int pr = prim_roundtrip(l.q.e);
+        const int64_t vb = (int64_t)r.b * L.V;
+        l.q.p0 = __ldg(L.pos4 + vb + r.ev.x);
+        l.q.p1 = __ldg(L.pos4 + vb + r.ev.y);
+        const int pr = prim_roundtrip(r.e);
         if (pr >= 0 && pr < L.E) l.craw = __ldg(p2c + pr);
     }
     return l;
@@ -224,11 +256,16 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
         }
     };
 
-    Lane cur = fetch(chunk0 + threadIdx.x, P, L, p2c);
+    Lane cur = fetch_pos(fetch_edge(chunk0 + threadIdx.x, P, L), L, p2c);
+    PreEdge pre = fetch_edge(chunk0 + kBinThreads + threadIdx.x, P, L);
     for (int j = 0; j < kBinPPT; ++j) {
-        Lane nxt;  // prefetch the next primitive of this thread
+        Lane nxt;  // positions of the next primitive (its edge came one iteration ago)
         nxt.valid = false;
-        if (j + 1 < kBinPPT) nxt = fetch(chunk0 + (int64_t)(j + 1) * kBinThreads + threadIdx.x, P, L, p2c);
+        nxt.craw = INT_MIN;
+        PreEdge pre2;  // the edge of the primitive after that
+        pre2.valid = false;
+        if (j + 2 < kBinPPT) pre2 = fetch_edge(chunk0 + (int64_t)(j + 2) * kBinThreads + threadIdx.x, P, L);
+        if (j + 1 < kBinPPT) nxt = fetch_pos(pre, L, p2c);
         if (cur.valid) {
             const Span s = dda_span(cur.q.p0, cur.q.p1, g.H, g.W);
             const int c = s.count > 0 ? cluster_checked(cur.craw, g.S) : -1;
@@ -373,6 +410,7 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
             }
         }
         cur = nxt;
+        pre = pre2;
     }
     __syncthreads();
     // exclusive scans over the slots: entry offsets and record ranks (4 slots per thread)
@@ -474,7 +512,7 @@ __global__ void __launch_bounds__(256) scatter_records(Ws w, int T) {
         if (w.nent[t] >= kHeavy) w.heavy[atomicAdd((unsigned long long*)(w.hdr + H_HEAVY), 1ull)] = (int)t;
 }
 
-__global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, Ws w, int32_t* __restrict__ bitset) {
+__global__ void __launch_bounds__(kRasterThreads, 3) dda_tile_raster_kernel(Geo g, Ws w, int32_t* __restrict__ bitset) {
     extern __shared__ uint32_t sm_bits[];
     const int TW = 1 << g.twl, TH = 1 << g.thl, TPX = TW * TH, S = g.S;
     const int rowstride = TPX + 1;
@@ -564,11 +602,10 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
             }
             continue;
         }
-        // Warps pull records from a shared counter.  Each warp loads 32 entries, scans their
-        // run lengths and lets each lane decode one fragment: major offset i, minor offset
-        // popc(steps & ((1 << i) - 1)) in the run's direction.  The next 32 entries (of this
-        // record, or the first of the warp's next record) are loaded before the current ones
-        // are decoded.
+        // Warps pull records from a shared counter.  Each lane replays one entry of 32: the
+        // first four fragments unrolled, longer runs lane by lane.  The next 32 entries (of
+        // this record, or the first of the warp's next record) are loaded before the current
+        // ones are replayed.
         int r = 0;
         if (lane == 0) r = atomicAdd(&s_rec, 1);
         r = __shfl_sync(0xffffffffu, r, 0);
@@ -595,54 +632,20 @@ __global__ void __launch_bounds__(kRasterThreads) dda_tile_raster_kernel(Geo g, 
                 uint32_t* col = sm_bits + (size_t)(c >> 5) * rowstride;
                 const uint32_t bit = 1u << (c & 31);
                 const int axis = (e.x >> 28) & 1, dir = (e.x >> 29) & 1 ? -1 : 1;
-                const int lp = (e.x >> 16) & 0xfff;
                 const unsigned steps = e.y >> 5;
-                // fragments 0..3 of this lane's run
-                {
-                    int lh = lp >> g.twl, lw = lp & (TW - 1);
+                // Every fragment of an entry lies in the tile (the bin pass cuts runs at tile
+                // borders), so a run walks one shared index: one pixel (x-major) or one tile row
+                // (y-major) per step, plus the minor move where the step bit is set.
+                const int inc_maj = axis ? TW : 1, inc_min = axis ? dir : dir * TW;
+                int pix = (e.x >> 16) & 0xfff;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        if (i < n && (unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW)
-                            atomicOr(col + lh * TW + lw, bit);
-                        const int st = (steps >> i) & 1;
-                        lh += axis ? 1 : (st ? dir : 0);
-                        lw += axis ? (st ? dir : 0) : 1;
-                    }
+                for (int i = 0; i < 4; ++i) {
+                    if (i < n && (unsigned)pix < (unsigned)TPX) atomicOr(col + pix, bit);
+                    pix += inc_maj + (((steps >> i) & 1) ? inc_min : 0);
                 }
-                // fragments 4.. of the longer runs, one per lane across the warp
-                const int rest = n > 4 ? n - 4 : 0;
-                if (__any_sync(0xffffffffu, rest > 0)) {
-                    int incl = rest;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += t;
-                    }
-                    const int total = __shfl_sync(0xffffffffu, incl, 31);
-                    const int excl = incl - rest;
-                    for (int f0 = 0; f0 < total; f0 += 32) {
-                        const int f = f0 + lane;
-                        int own = 0;  // first lane whose inclusive count exceeds f
-#pragma unroll
-                        for (int step = 16; step; step >>= 1) {
-                            const int v = __shfl_sync(0xffffffffu, incl, own + step - 1);
-                            if (v <= f) own += step;
-                        }
-                        own = min(own, 31);
-                        const int i = 4 + f - __shfl_sync(0xffffffffu, excl, own);
-                        const uint32_t ex = __shfl_sync(0xffffffffu, e.x, own);
-                        const uint32_t ey = __shfl_sync(0xffffffffu, e.y, own);
-                        if (f < total) {
-                            const int cc = ex & 0xffff;
-                            const int lpo = (ex >> 16) & 0xfff;
-                            const int mv = __popc((ey >> 5) & ((1u << i) - 1u)) * ((ex >> 29) & 1 ? -1 : 1);
-                            int lh = lpo >> g.twl, lw = lpo & (TW - 1);
-                            if ((ex >> 28) & 1) { lh += i; lw += mv; }
-                            else { lw += i; lh += mv; }
-                            if ((unsigned)lh < (unsigned)TH && (unsigned)lw < (unsigned)TW)
-                                atomicOr(sm_bits + (size_t)(cc >> 5) * rowstride + lh * TW + lw, 1u << (cc & 31));
-                        }
-                    }
+                for (int i = 4; i < n; ++i) {  // the longer runs, lane by lane
+                    if ((unsigned)pix < (unsigned)TPX) atomicOr(col + pix, bit);
+                    pix += inc_maj + (((steps >> i) & 1) ? inc_min : 0);
                 }
                 e = en;
             }
