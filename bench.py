@@ -263,7 +263,7 @@ def run_ours(args):
     dins = [(torch.empty_like(pos), torch.empty_like(edges), torch.empty_like(e2c)) for _ in range(2)]
     douts = [out, torch.empty_like(out)]
     s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-    e2e_steps = max(3, min(args.steps, 10))
+    e2e_steps = max(3, min(args.steps, 300))
 
     def e2e_run(k):
         ev_in = [torch.cuda.Event() for _ in range(k)]

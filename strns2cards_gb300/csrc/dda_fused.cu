@@ -197,6 +197,10 @@ __device__ __forceinline__ Lane fetch_pos(const PreEdge& r, const Lines& L, cons
     return l;
 }
 
+// floor(x) for |x| < 2^22 without a conversion instruction: x + 1.5 * 2^23 rounded down is
+// an integer in [2^23, 2^24), whose bits less those of 1.5 * 2^23 are floor(x)
+__device__ __forceinline__ int floor_small(float x) { return __float_as_int(__fadd_rd(x, 12582912.0f)) - 0x4B400000; }
+
 // cluster_of on a prefetched entry
 __device__ __forceinline__ int cluster_checked(int craw, int S) { return craw >= 0 && craw < 32 * S ? craw : -1; }
 
@@ -294,16 +298,18 @@ __global__ void __launch_bounds__(kBinThreads) dda_bin_kernel(int64_t P, Lines L
                 // interior samples need no clamping (off0 < 1.5 <= k + 0.5 < off1).
                 const int dir = s.slope >= 0.f ? 1 : -1;
                 bool simple = zfast && isfinite(s.slope) && last <= 32 && m0 == f2i(smaj) && ml == m0 + last &&
-                              m0 >= 0 && ml < nmaj && min(n0, nl) >= 0 && max(n0, nl) < nmin;
+                              m0 >= 0 && ml < nmaj && min(n0, nl) >= 0 && max(n0, nl) < nmin && nmin <= (1 << 21);
                 // Phase 1: one bit per step k-1 -> k: does the minor pixel move?  Interior
-                // samples are d = k + 0.5 exactly; the last fragment was sampled above.
+                // samples are d = k + 0.5 exactly; the last fragment was sampled above.  The
+                // interior minor coordinates lie between the end ones, inside [0, nmin) with
+                // nmin <= 2^21, so floor_small gives __float2int_rd's result.
                 uint32_t bits = 0;
                 if (simple) {
                     int prev = n0;
                     bool bad = false;
                     float kf = 1.5f;
                     for (int k = 1; k < last; ++k, kf += 1.0f) {
-                        const int in = __float2int_rd(__fadd_rn(smin, __fmul_rn(kf, s.slope)));
+                        const int in = floor_small(__fadd_rn(smin, __fmul_rn(kf, s.slope)));
                         const int dm = in - prev;
                         bits |= (uint32_t)(dm != 0) << (k - 1);
                         bad |= (dm != 0) & (dm != dir);
