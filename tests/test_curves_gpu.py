@@ -118,3 +118,16 @@ def test_device_resampling_equals_host():
     bad[8] += 1
     out = np_(s2c.resample_strands_by_arclength(cu(bad), cu(pts), 10))
     assert np.isnan(out[7]).all()
+
+
+@pytest.mark.parametrize("n", [16384, 16385, 40000])
+def test_device_resampling_scan_sizes(n):
+    """The strand offsets come from the device scan: one CTA up to 16,384 strands, the
+    three-launch scan above; both give the host's offsets."""
+    import strns2cards_gb300 as s2c
+    rng = np.random.default_rng(n)
+    counts = rng.integers(2, 12, size=n).astype(np.int32)
+    pts = np.cumsum(rng.normal(scale=0.02, size=(int(counts.sum()), 3)), 0).astype(np.float32)
+    host = s2c.resample_strands_by_arclength(counts, pts, 7)
+    dev = s2c.resample_strands_by_arclength(cu(counts), cu(pts), 7)
+    assert np.array_equal(np_(dev), host)
