@@ -12,8 +12,9 @@
 //           as runs: one 8-byte entry holds the cluster, the first pixel inside a screen
 //           tile and one bit per further step along the minor axis, so a run needs no
 //           floating point to replay.  Entries are grouped by tile in shared memory
-//           (hash of tile ids, warp-aggregated counters), written contiguously per tile,
-//           and one (tile, start, count) record per touched tile goes to a record pool.
+//           (hash of tile ids, a shared counter per tile whose atomicAdd gives each entry
+//           its place), written contiguously per tile, and one (tile, start, count, rank)
+//           record per touched tile goes to a record pool.
 //  scan     exclusive offsets of the per-tile record counts.
 //  scatter  records sorted by tile (each carries its rank in the tile from the bin pass);
 //           tiles with many entries listed first.
