@@ -70,3 +70,31 @@ def test_argument_errors_come_back_as_status_without_a_gpu(lib_built):
     assert L.s2c_align_strands(0, 8, None, 0, None, None, None, t3, 0.05, None, None, None) == 0
     assert L.s2c_align_strands_max_points() >= 64
     assert L.s2c_build_edges_device_workspace_size(0, 0) > 0
+
+
+def test_dda_cluster_bitset_argument_errors_without_a_gpu(lib_built):
+    """The headline entry rejects bad arguments on the host, before any launch: sizes,
+    slot count, null and misaligned pointers (INVALID), a short workspace (WORKSPACE), and
+    a problem too large for the no-alloc variant's fixed scratch (INVALID).  The pointers
+    below are aligned addresses that are never dereferenced."""
+    from strns2cards_gb300 import _lib
+    L = _lib.lib()
+    pos, edges, p2c, bits, ws = 0x10000, 0x20000, 0x30000, 0x40000, 0x50000
+    ok = dict(P=1000, ids=None, H=64, W=64, B=1, V=2000, pos=pos, E=1000, edges=edges, p2c=p2c, S=2, bits=bits,
+              ws=ws, wsb=0)
+
+    def call(**kw):
+        a = dict(ok, **kw)
+        return L.s2c_dda_cluster_bitset(a["P"], a["ids"], a["H"], a["W"], a["B"], a["V"], a["pos"], a["E"], a["edges"],
+                                        a["p2c"], a["S"], a["bits"], a["ws"], a["wsb"], None)
+
+    for kw in (dict(P=-1), dict(H=0), dict(W=40000), dict(B=0), dict(P=1001),    # P > B*E without edge ids
+               dict(pos=None), dict(edges=None), dict(S=0), dict(S=2049), dict(bits=None),
+               dict(bits=bits + 4), dict(pos=pos + 4), dict(edges=edges + 4), dict(p2c=None)):
+        assert call(**kw) == _lib.S2C_ERR_INVALID, kw
+        assert L.s2c_last_error(), kw
+    assert call() == _lib.S2C_ERR_WORKSPACE                                       # workspace of 0 bytes
+    assert call(ws=None, wsb=1 << 30) == _lib.S2C_ERR_WORKSPACE
+    assert L.s2c_dda_cluster_bitset_noalloc(5_000_000, None, 1024, 1024, 1, 5_050_000, pos, 5_000_000, edges, p2c, 64,
+                                            bits, None) == _lib.S2C_ERR_INVALID
+    assert b"fixed" in L.s2c_last_error()
