@@ -109,8 +109,12 @@ S2C_API s2c_status s2c_dda_cluster_bitset(int64_t num_prims, const int32_t* edge
  * until the process exits.  Problems whose s2c_dda_cluster_bitset_workspace_size()
  * exceeds 32 MiB are rejected with S2C_ERR_INVALID (about 1.4M segments at 1024x1024).
  * No cudaMalloc/cudaFree.  The first call on each device looks up the array's device
- * address (make it before any stream capture).  All calls share the array, so calls that
- * overlap on the GPU (different streams, or different host threads) race; serialise them. */
+ * address (make it before any stream capture) and keeps it for the process: do not call
+ * this entry after cudaDeviceReset (or after the primary context was released and made
+ * again), where that address is no longer valid.  All calls share the array, so calls that
+ * overlap on the GPU (different streams, or different host threads) race; serialise them.
+ * s2c_dda_cluster_bitset_stats needs the workspace pointer and so is not available here.
+ * Bad arguments are rejected on the host before any CUDA call, as for the entry above. */
 S2C_API s2c_status s2c_dda_cluster_bitset_noalloc(int64_t num_prims, const int32_t* edge_ids, int H,
                                                   int W, int B, int V, const float* pos, int E,
                                                   const int32_t* edges, const int32_t* prim2cluster,

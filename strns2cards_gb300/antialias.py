@@ -81,7 +81,11 @@ class _TargetPlanesCache:
         cur = torch.cuda.current_stream(target.device)
         if hit is not None:
             if hit[1] != cur:
-                cur.wait_stream(hit[1])   # planes written on another stream
+                # planes written on another stream: wait for them, and tell the caching
+                # allocator that this stream reads them too, so that dropping the entry
+                # later cannot hand the block out while this stream's kernels still read it
+                cur.wait_stream(hit[1])
+                hit[0].record_stream(cur)
             return hit[0]
         pl = _core.bitset_to_planes(target)
         self._entries.append((weakref.ref(target), target._version, target.data_ptr(), pl, cur))

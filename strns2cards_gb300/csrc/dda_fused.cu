@@ -748,15 +748,27 @@ extern "C" size_t s2c_dda_cluster_bitset_workspace_size(int64_t P, int B, int H,
     return fixed + (size_t)entries * sizeof(uint2);
 }
 
+namespace s2c {
+// host-side argument checks of both bitset entries (no CUDA call)
+static s2c_status check_bitset_call(int64_t P, const int32_t* edge_ids, int H, int W, int B, int V, const float* pos,
+                                    int E, const int32_t* edges, const int32_t* p2c, int S, const int32_t* bitset,
+                                    const char* who) {
+    if (s2c_status s = check_lines(P, edge_ids, H, W, B, V, pos, E, edges, who)) return s;
+    S2C_REQUIRE(S > 0 && S <= 2048, "%s: slot count must be in [1, 2048] (K <= 65536)", who);
+    S2C_REQUIRE(bitset && ((uintptr_t)bitset & 15) == 0, "%s: bitset must be 16-byte aligned", who);
+    S2C_REQUIRE(P == 0 || p2c, "%s: null prim2cluster", who);
+    const Geo g = make_geo(B, H, W, S);
+    S2C_REQUIRE((int64_t)B * g.tiles_x * g.tiles_y < (1LL << 31), "%s: too many tiles", who);
+    return S2C_OK;
+}
+}  // namespace s2c
+
 extern "C" s2c_status s2c_dda_cluster_bitset(int64_t P, const int32_t* edge_ids, int H, int W, int B, int V,
                                              const float* pos, int E, const int32_t* edges, const int32_t* p2c,
                                              int S, int32_t* bitset, void* ws, size_t ws_bytes, s2c_stream stream) {
-    if (s2c_status s = check_lines(P, edge_ids, H, W, B, V, pos, E, edges, "dda_cluster_bitset")) return s;
-    S2C_REQUIRE(S > 0 && S <= 2048, "dda_cluster_bitset: slot count must be in [1, 2048] (K <= 65536)");
-    S2C_REQUIRE(bitset && ((uintptr_t)bitset & 15) == 0, "dda_cluster_bitset: bitset must be 16-byte aligned");
-    S2C_REQUIRE(P == 0 || p2c, "dda_cluster_bitset: null prim2cluster");
+    if (s2c_status s = check_bitset_call(P, edge_ids, H, W, B, V, pos, E, edges, p2c, S, bitset, "dda_cluster_bitset"))
+        return s;
     const Geo g = make_geo(B, H, W, S);
-    S2C_REQUIRE((int64_t)B * g.tiles_x * g.tiles_y < (1LL << 31), "dda_cluster_bitset: too many tiles");
     Ws w;
     const size_t fixed = layout(ws, ws_bytes, P, g, w);
     if (!ws || ws_bytes < fixed + 4096 * sizeof(uint2)) {
@@ -867,6 +879,10 @@ extern "C" s2c_status s2c_dda_cluster_bitset_noalloc(int64_t P, const int32_t* e
                                                      const float* pos, int E, const int32_t* edges,
                                                      const int32_t* p2c, int S, int32_t* bitset,
                                                      s2c_stream stream) {
+    // every argument check before the first CUDA call, as the workspace entry does
+    if (s2c_status s = check_bitset_call(P, edge_ids, H, W, B, V, pos, E, edges, p2c, S, bitset,
+                                         "dda_cluster_bitset_noalloc"))
+        return s;
     const size_t need = s2c_dda_cluster_bitset_workspace_size(P, B, H, W, S);
     if (need > kFixedScratchBytes) {
         set_error("dda_cluster_bitset_noalloc: this problem needs %zu bytes of scratch, more than the fixed %zu "

@@ -88,11 +88,20 @@ def test_dda_cluster_bitset_argument_errors_without_a_gpu(lib_built):
         return L.s2c_dda_cluster_bitset(a["P"], a["ids"], a["H"], a["W"], a["B"], a["V"], a["pos"], a["E"], a["edges"],
                                         a["p2c"], a["S"], a["bits"], a["ws"], a["wsb"], None)
 
+    def call_noalloc(**kw):
+        a = dict(ok, **kw)
+        return L.s2c_dda_cluster_bitset_noalloc(a["P"], a["ids"], a["H"], a["W"], a["B"], a["V"], a["pos"], a["E"],
+                                                a["edges"], a["p2c"], a["S"], a["bits"], None)
+
+    # both entries reject the same bad arguments on the host, before any CUDA call (so
+    # these run without a GPU and name the entry in the message)
     for kw in (dict(P=-1), dict(H=0), dict(W=40000), dict(B=0), dict(P=1001),    # P > B*E without edge ids
                dict(pos=None), dict(edges=None), dict(S=0), dict(S=2049), dict(bits=None),
                dict(bits=bits + 4), dict(pos=pos + 4), dict(edges=edges + 4), dict(p2c=None)):
         assert call(**kw) == _lib.S2C_ERR_INVALID, kw
         assert L.s2c_last_error(), kw
+        assert call_noalloc(**kw) == _lib.S2C_ERR_INVALID, kw
+        assert b"dda_cluster_bitset_noalloc" in L.s2c_last_error(), kw
     assert call() == _lib.S2C_ERR_WORKSPACE                                       # workspace of 0 bytes
     assert call(ws=None, wsb=1 << 30) == _lib.S2C_ERR_WORKSPACE
     assert L.s2c_dda_cluster_bitset_noalloc(5_000_000, None, 1024, 1024, 1, 5_050_000, pos, 5_000_000, edges, p2c, 64,

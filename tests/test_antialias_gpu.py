@@ -206,3 +206,33 @@ def test_target_planes_cache_is_exact_and_follows_writes():
     assert len(target_planes_cache._entries) == 1
     with pytest.raises(RuntimeError):
         s2c.antialiased_cluster_bitset_grad(bits, bits[:, :, :-1].contiguous(), pos, tri, edges, e2t, e2c, 7.0, 0.5)
+
+
+def test_target_planes_cache_used_from_another_stream_survives_eviction():
+    # planes cached on the default stream, read by a gradient queued behind a long sleep on
+    # a second stream; the target dies and its entry is dropped while that stream still
+    # waits, and same-sized blocks are then allocated and overwritten on the default
+    # stream.  The second stream must still read the target's planes.
+    import gc
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    from strns2cards_gb300.antialias import target_planes_cache
+    a = golden("antialias.npz")
+    bits, tgt, pos, tri, edges, e2t, e2c = (cu(a[k]) for k in ("bitset", "target", "pos", "tri", "edges", "edge2tri",
+                                                                 "edge2cluster"))
+    target_planes_cache.clear()
+    ref = _core.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    s2c.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)   # caches tgt's planes
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        torch.cuda._sleep(100_000_000)   # keeps the side stream busy while the host goes on
+        g = s2c.antialiased_cluster_bitset_grad(bits, tgt, pos, tri, edges, e2t, e2c, 7.0, 0.5)
+    del tgt
+    gc.collect()
+    target_planes_cache.planes(bits)          # drops the dead entry (its planes are freed)
+    junk = [torch.full_like(_core.bitset_to_planes(bits), -1) for _ in range(4)]
+    torch.cuda.synchronize()
+    assert torch.equal(g, ref)
+    del junk
+    target_planes_cache.clear()

@@ -53,6 +53,30 @@ def test_noalloc_matches_workspace_entry_on_two_calls(lib_built):
     assert torch.equal(ref2, got2)
 
 
+def test_noalloc_matches_workspace_entry_at_its_size_limit(lib_built):
+    # the largest strand scene (100-point strands, 1024x1024, K = 2048) whose scratch still
+    # fits the fixed 32 MiB: the case where the entry pool is nearly full
+    from strns2cards_gb300 import _lib
+    from strns2cards_gb300 import synthetic as syn
+    L = _lib.lib()
+    limit = 32 << 20
+    n_strands = 1
+    while L.s2c_dda_cluster_bitset_workspace_size((2 * n_strands) * 99, 1, 1024, 1024, 64) <= limit:
+        n_strands *= 2
+    lo, hi = n_strands, 2 * n_strands
+    while hi - lo > 1:
+        mid = (lo + hi) // 2
+        if L.s2c_dda_cluster_bitset_workspace_size(mid * 99, 1, 1024, 1024, 64) <= limit:
+            lo = mid
+        else:
+            hi = mid
+    assert L.s2c_dda_cluster_bitset_workspace_size((lo + 1) * 99, 1, 1024, 1024, 64) > limit
+    sc = syn.strand_scene(lo, 100, per_cluster=25, num_views=1, seed=3)
+    ref, got = _run_pair(sc, 1024, 1024, 2048)
+    assert torch.equal(ref, got)
+    assert int(ref.ne(0).sum()) > 100_000
+
+
 def test_noalloc_rejects_problems_beyond_its_scratch(lib_built):
     from strns2cards_gb300 import _lib
     L = _lib.lib()
