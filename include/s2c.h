@@ -194,12 +194,16 @@ S2C_API s2c_status s2c_interpolate_triangle_attributes(int B, int H, int W, int 
                                                        s2c_stream stream);
 
 /* replaces: backward_interpolate_triangle_attributes (pystrns2cards.cpp:417-438;
- * rasterize.cu:402-472).  d_attr (V, C) accumulated with float atomics. */
+ * rasterize.cu:402-472).  d_attr (V, C) += sum over pixels of b_i * grad.  acc64: NULL ->
+ * float atomics straight into d_attr (the reference's arithmetic); else a caller buffer of
+ * V*C doubles (8-byte aligned, cleared here): the exact FP32 products are summed in FP64
+ * and each sum is rounded once into d_attr. */
 S2C_API s2c_status s2c_backward_interpolate_triangle_attributes(int B, int H, int W, int C,
                                                                 const float* rast,
                                                                 const float* d_image, int T,
                                                                 const int32_t* tri, int V,
-                                                                float* d_attr, s2c_stream stream);
+                                                                float* d_attr, double* acc64,
+                                                                s2c_stream stream);
 
 /* replaces: dda_interpolate_attributes (pystrns2cards.cpp:613-647; dda.cu:258-298) */
 S2C_API s2c_status s2c_dda_interpolate_attributes(int B, int H, int W, int C, const float* rast,
@@ -207,11 +211,13 @@ S2C_API s2c_status s2c_dda_interpolate_attributes(int B, int H, int W, int C, co
                                                   const int32_t* edges, float* image,
                                                   s2c_stream stream);
 
-/* replaces: backward_dda_interpolate_attributes (pystrns2cards.cpp:649-680; dda.cu:300-342) */
+/* replaces: backward_dda_interpolate_attributes (pystrns2cards.cpp:649-680; dda.cu:300-342).
+ * acc64 as for s2c_backward_interpolate_triangle_attributes. */
 S2C_API s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int W, int C,
                                                            const float* rast, const float* d_image,
                                                            int E, const int32_t* edges, int V,
-                                                           float* d_attr, s2c_stream stream);
+                                                           float* d_attr, double* acc64,
+                                                           s2c_stream stream);
 
 /* ---------------------------------------------------------------------------------- *
  * stream compaction                                                                   *

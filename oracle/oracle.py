@@ -386,57 +386,101 @@ def lbs_bind(x, guides, tau=0.01):
     return idx, w
 
 
-def lbs_forward(x, idx, w, M):
+def lbs_forward(x, idx, w, M, chunk=1 << 19):
+    """y_v = sum_k w_vk (A_k x_v + t_k) in FP64, in chunks of vertices."""
     x = np.asarray(x, np.float64).reshape(-1, 3)
-    xh = np.concatenate([x, np.ones((x.shape[0], 1))], 1)
     M = np.asarray(M, np.float64)
-    ok = idx >= 0
-    Mi = M[np.where(ok, idx, 0)]                               # (Nv, 4, 3, 4)
-    yk = np.einsum("vkrc,vc->vkr", Mi, xh)
-    return np.einsum("vk,vkr->vr", np.where(ok, w, 0.0), yk)
+    idx = np.asarray(idx)
+    w = np.asarray(w, np.float64)
+    y = np.zeros((x.shape[0], 3), np.float64)
+    for a in range(0, x.shape[0], chunk):
+        b = min(a + chunk, x.shape[0])
+        xh = np.concatenate([x[a:b], np.ones((b - a, 1))], 1)
+        ok = idx[a:b] >= 0
+        Mi = M[np.where(ok, idx[a:b], 0)]                       # (n, 4, 3, 4)
+        yk = np.einsum("vkrc,vc->vkr", Mi, xh)
+        y[a:b] = np.einsum("vk,vkr->vr", np.where(ok, w[a:b], 0.0), yk)
+    return y
 
 
-def lbs_backward(x, idx, w, M, gy):
+def lbs_backward(x, idx, w, M, gy, chunk=1 << 19):
+    """dM_g = sum over bindings (v, k) to guide g of w_vk gy_v [x_v; 1]^T, and
+    dx_v = sum_k w_vk A_k^T gy_v, in FP64 (chunks of vertices; per-guide sums by bincount)."""
     x = np.asarray(x, np.float64).reshape(-1, 3)
-    xh = np.concatenate([x, np.ones((x.shape[0], 1))], 1)
     M = np.asarray(M, np.float64)
-    gy = np.asarray(gy, np.float64)
-    ok = idx >= 0
-    wz = np.where(ok, w, 0.0)
+    gy = np.asarray(gy, np.float64).reshape(-1, 3)
+    idx = np.asarray(idx)
+    w = np.asarray(w, np.float64)
+    G = M.shape[0]
     dM = np.zeros_like(M)
-    contrib = np.einsum("vk,vr,vc->vkrc", wz, gy, xh)
-    np.add.at(dM, np.where(ok, idx, 0).reshape(-1), contrib.reshape(-1, 3, 4) * ok.reshape(-1, 1, 1))
-    A = M[np.where(ok, idx, 0)][..., :3]                        # (Nv, 4, 3, 3)
-    dx = np.einsum("vk,vkrc,vr->vc", wz, A, gy)
+    dx = np.zeros((x.shape[0], 3), np.float64)
+    for a in range(0, x.shape[0], chunk):
+        b = min(a + chunk, x.shape[0])
+        xh = np.concatenate([x[a:b], np.ones((b - a, 1))], 1)
+        ok = idx[a:b] >= 0
+        wz = np.where(ok, w[a:b], 0.0)
+        ii = np.where(ok, idx[a:b], 0).reshape(-1)
+        for r in range(3):
+            for c in range(4):
+                dM[:, r, c] += np.bincount(ii, weights=(wz * (gy[a:b, r] * xh[:, c])[:, None]).reshape(-1),
+                                           minlength=G)
+        A = M[np.where(ok, idx[a:b], 0)][..., :3]                # (n, 4, 3, 3)
+        dx[a:b] = np.einsum("vk,vkrc,vr->vc", wz, A, gy[a:b])
     return dM, dx
 
 
 # ---- barycentric derivatives (new output): the forward's clip-space edge functions
 # (rasterize.cu:144-156) at the pixel centre, differentiated in FP64
-def barycentric_derivatives(rast, pos, tri):
+def barycentric_derivatives(rast, pos, tri, with_mag=False, chunk=1 << 20):
+    """d(b0, b1)/d(x, y) in FP64 (out[..., 0:2] = db0/dx, db0/dy; out[..., 2:4] = db1/dx,
+    db1/dy).  With ``with_mag``, also a first-order condition scale per element: the error
+    that one unit roundoff in every input and intermediate of the formula would cause,
+    propagated with absolute values (sums and products add their terms' magnitudes; a
+    quotient n / d adds |n| / |d| times the relative error of d)."""
     rast = np.asarray(rast, np.float32)
     B, H, W, _ = rast.shape
     out = np.zeros((B, H, W, 4), np.float64)
+    mag = np.zeros((B, H, W, 4), np.float64) if with_mag else None
     t = rast[..., 3].astype(np.int64) - 1
-    b, y, x = np.nonzero(t >= 0)
-    tt = t[b, y, x]
-    # pixel centre in NDC, in FP32 as the forward computes it
-    px = (np.float32(-1) + (np.float32(2) * (x.astype(np.float32) + np.float32(0.5))) / np.float32(W)).astype(np.float64)
-    py = (np.float32(-1) + (np.float32(2) * (y.astype(np.float32) + np.float32(0.5))) / np.float32(H)).astype(np.float64)
-    P = np.asarray(pos, np.float64)[b[:, None], np.asarray(tri)[tt]]          # (n, 3, 4)
-    qx = P[..., 0] - px[:, None] * P[..., 3]
-    qy = -P[..., 1] - py[:, None] * P[..., 3]
+    bs, ys, xs = np.nonzero(t >= 0)
+    pos64 = np.asarray(pos, np.float64)
+    tri = np.asarray(tri)
     j, k = [1, 2, 0], [2, 0, 1]
-    A = qx[:, j] * qy[:, k] - qy[:, j] * qx[:, k]                               # (n, 3)
-    dAx = P[:, j, 3] * P[:, k, 1] - P[:, k, 3] * P[:, j, 1]
-    dAy = P[:, j, 3] * P[:, k, 0] - P[:, k, 3] * P[:, j, 0]
-    S = A.sum(1)
-    ok = S != 0
-    bb = A / np.where(ok, S, 1.0)[:, None]
-    for i in range(2):
-        out[b, y, x, 2 * i] = np.where(ok, (dAx[:, i] - bb[:, i] * dAx.sum(1)) / np.where(ok, S, 1.0) * (2.0 / W), 0.0)
-        out[b, y, x, 2 * i + 1] = np.where(ok, (dAy[:, i] - bb[:, i] * dAy.sum(1)) / np.where(ok, S, 1.0) * (2.0 / H), 0.0)
-    return out
+    for c0 in range(0, bs.shape[0], chunk):
+        b, y, x = bs[c0:c0 + chunk], ys[c0:c0 + chunk], xs[c0:c0 + chunk]
+        tt = t[b, y, x]
+        # pixel centre in NDC, in FP32 as the forward computes it
+        px = (np.float32(-1) + (np.float32(2) * (x.astype(np.float32) + np.float32(0.5))) / np.float32(W)).astype(np.float64)
+        py = (np.float32(-1) + (np.float32(2) * (y.astype(np.float32) + np.float32(0.5))) / np.float32(H)).astype(np.float64)
+        P = pos64[b[:, None], tri[tt]]                                               # (n, 3, 4)
+        qx = P[..., 0] - px[:, None] * P[..., 3]
+        qy = -P[..., 1] - py[:, None] * P[..., 3]
+        A = qx[:, j] * qy[:, k] - qy[:, j] * qx[:, k]                               # (n, 3)
+        dAx = P[:, j, 3] * P[:, k, 1] - P[:, k, 3] * P[:, j, 1]
+        dAy = P[:, j, 3] * P[:, k, 0] - P[:, k, 3] * P[:, j, 0]
+        S = A.sum(1)
+        ok = S != 0
+        Ss = np.where(ok, S, 1.0)
+        bb = A / Ss[:, None]
+        sxy = (2.0 / W, 2.0 / H)
+        if with_mag:
+            mqx = np.abs(P[..., 0]) + np.abs(px[:, None] * P[..., 3])
+            mqy = np.abs(P[..., 1]) + np.abs(py[:, None] * P[..., 3])
+            mA = mqx[:, j] * mqy[:, k] + mqy[:, j] * mqx[:, k]
+            mS = mA.sum(1)
+            mdx = np.abs(P[:, j, 3] * P[:, k, 1]) + np.abs(P[:, k, 3] * P[:, j, 1])
+            mdy = np.abs(P[:, j, 3] * P[:, k, 0]) + np.abs(P[:, k, 3] * P[:, j, 0])
+        for i in range(2):
+            for d, (dA, sc) in enumerate(((dAx, sxy[0]), (dAy, sxy[1]))):
+                sd = dA.sum(1)
+                N = dA[:, i] - bb[:, i] * sd
+                out[b, y, x, 2 * i + d] = np.where(ok, N / Ss * sc, 0.0)
+                if with_mag:
+                    md = (mdx if d == 0 else mdy)
+                    # |bb_i| times its relative error (A_i / S): mag(A_i) / |S| + |bb_i| mag(S) / |S|
+                    mN = md[:, i] + np.abs(bb[:, i]) * md.sum(1) + np.abs(sd) * (mA[:, i] + np.abs(bb[:, i]) * mS) / np.abs(Ss)
+                    mag[b, y, x, 2 * i + d] = np.where(ok, (mN / np.abs(Ss) + np.abs(N) * mS / Ss ** 2) * sc, 0.0)
+    return (out, mag) if with_mag else out
 
 
 # ---- strand frames and wisp alignment (curve_utils.py:9-165, 243-308, 481-607), FP64 numpy
@@ -621,3 +665,102 @@ def align_wisp(strands, beta):
     arc_s = np.concatenate([np.zeros((p.shape[0], 1), np.float32),
                             np.cumsum(np.linalg.norm(s_rot[:, 1:] - s_rot[:, :-1], axis=-1), 1)], 1)
     return skinning(s_rot, arc_s, h_rot, canon, Rl, beta), h_rot, li
+
+
+# ---- condition scales of the float outputs -------------------------------------------
+# Every float output on this path is a sum of products (weights and barycentrics are
+# non-negative).  FP32 evaluation, here or in the reference, is accurate relative to the
+# sum of the terms' magnitudes, which equals |value| only where no terms cancel.  Each
+# function below evaluates the same FP64 formula on absolute values: per output element,
+# sum |term|, where a factor that the formula itself forms by a subtraction (b2 = 1 - b0 -
+# b1, t0 = 1 - t1) counts with the magnitude it was formed from.  The parity tests bound
+# |got - FP64| by 1e-5 x max(|FP64 value|, this scale).
+def _covered(rast, prim_count):
+    r = np.asarray(rast, np.float32).reshape(-1, 4)
+    t = r[:, 3].astype(np.int64) - 1
+    ok = (t >= 0) & (t < prim_count)
+    return np.nonzero(ok)[0], r[ok].astype(np.float64), t[ok]
+
+
+def interpolate_mag(rast, attr, tri):
+    """|b0 a0| + |b1 a1| + (1 + |b0| + |b1|) |a2| (rasterize.cu:367-400): b2 = 1 - b0 - b1 is
+    itself a rounded difference, so its term is scaled by what it was computed from."""
+    rast = np.asarray(rast, np.float32)
+    a = np.abs(np.asarray(attr, np.float64))
+    tri = np.asarray(tri, np.int64)
+    B, H, W, _ = rast.shape
+    out = np.zeros((B * H * W, a.shape[1]), np.float64)
+    p, r, t = _covered(rast, tri.shape[0])
+    v = tri[t]
+    b0, b1 = np.abs(r[:, :1]), np.abs(r[:, 1:2])
+    out[p] = b0 * a[v[:, 0]] + b1 * a[v[:, 1]] + (1.0 + b0 + b1) * a[v[:, 2]]
+    return out.reshape(B, H, W, -1)
+
+
+def _scatter_mag(V, C, idx_w):
+    d = np.zeros((V, C), np.float64)
+    for vi, w in idx_w:
+        for c in range(C):
+            d[:, c] += np.bincount(vi, weights=w[:, c], minlength=V)
+    return d
+
+
+def interpolate_backward_mag(rast, d_image, tri, V):
+    """sum over pixels of |g| b0, |g| b1 and |g| (1 + b0 + b1) into the three vertices"""
+    rast = np.asarray(rast, np.float32)
+    tri = np.asarray(tri, np.int64)
+    g = np.abs(np.asarray(d_image, np.float64)).reshape(-1, np.asarray(d_image).shape[-1])
+    p, r, t = _covered(rast, tri.shape[0])
+    v, gp = tri[t], g[p]
+    b0, b1 = np.abs(r[:, :1]), np.abs(r[:, 1:2])
+    return _scatter_mag(int(V), g.shape[1], [(v[:, 0], gp * b0), (v[:, 1], gp * b1), (v[:, 2], gp * (1.0 + b0 + b1))])
+
+
+def dda_interpolate_mag(rast, attr, edges):
+    """(1 + |t1|) |a0| + |t1| |a1| (dda.cu:258-298; t0 = 1 - t1 rounded)"""
+    rast = np.asarray(rast, np.float32)
+    a = np.abs(np.asarray(attr, np.float64))
+    edges = np.asarray(edges, np.int64)
+    B, H, W, _ = rast.shape
+    out = np.zeros((B * H * W, a.shape[1]), np.float64)
+    p, r, e = _covered(rast, edges.shape[0])
+    v = edges[e]
+    t1 = np.abs(r[:, 1:2])
+    out[p] = (1.0 + t1) * a[v[:, 0]] + t1 * a[v[:, 1]]
+    return out.reshape(B, H, W, -1)
+
+
+def dda_interpolate_backward_mag(rast, d_image, edges, V):
+    rast = np.asarray(rast, np.float32)
+    edges = np.asarray(edges, np.int64)
+    g = np.abs(np.asarray(d_image, np.float64)).reshape(-1, np.asarray(d_image).shape[-1])
+    p, r, e = _covered(rast, edges.shape[0])
+    v, gp = edges[e], g[p]
+    t1 = np.abs(r[:, 1:2])
+    return _scatter_mag(int(V), g.shape[1], [(v[:, 0], gp * (1.0 + t1)), (v[:, 1], gp * t1)])
+
+
+def smooth_strands_mag(strands, arclength, beta):
+    """sum_j w_j |x_j| / sum_j w_j (curve_utils.cu:24-68; w_j > 0)"""
+    return smooth_strands(np.abs(np.asarray(strands, np.float32)), arclength, beta)
+
+
+def skinning_mag(strands, arclength, handles, canonical, R, beta):
+    """sum_j w_j (|R_j| (|x_i| + |h_j|) + |c_j|) / sum_j w_j (curve_utils.cu:70-131)"""
+    a32 = lambda a: np.abs(np.asarray(a, np.float32))
+    return skinning(a32(strands), arclength, -a32(handles), a32(canonical), a32(R), beta)
+
+
+def card_laplacian_smooth_mag(verts, quad_edges, verts_per_card, lam=0.5, steps=10):
+    """p <- (1 - lam) p + lam mean(neighbours) has non-negative coefficients for lam in
+    [0, 1]: the same iteration on |p|"""
+    return card_laplacian_smooth(np.abs(np.asarray(verts, np.float64)), quad_edges, verts_per_card, lam, steps)
+
+
+def lbs_forward_mag(x, idx, w, M):
+    return lbs_forward(np.abs(np.asarray(x, np.float64)), idx, w, np.abs(np.asarray(M, np.float64)))
+
+
+def lbs_backward_mag(x, idx, w, M, gy):
+    return lbs_backward(np.abs(np.asarray(x, np.float64)), idx, w, np.abs(np.asarray(M, np.float64)),
+                        np.abs(np.asarray(gy, np.float64)))

@@ -200,8 +200,10 @@ def backward_interpolate_triangle_attributes(rast, d_image, tri, d_attr) -> None
     _cuda(rast, d_image, tri, d_attr, msg="All tensors must be on a CUDA device")
     B, H, W, _ = rast.shape
     V, C = d_attr.shape
+    # FP64 sums of the exact FP32 products, rounded once into d_attr
+    acc = torch.empty(V * C, dtype=torch.float64, device=d_attr.device)
     call("s2c_backward_interpolate_triangle_attributes", B, H, W, C, ptr(rast), ptr(d_image), tri.shape[0], ptr(tri), V,
-         ptr(d_attr), _stream(rast))
+         ptr(d_attr), ptr(acc), _stream(rast))
 
 
 def dda_interpolate_attributes(rast_dda, attr, edges, image) -> None:
@@ -230,8 +232,9 @@ def backward_dda_interpolate_attributes(rast_dda, d_image, edges, d_attr) -> Non
         raise RuntimeError("`d_image` must have shape [B, H, W, C] matching rast_dda")
     if d_attr.shape[1] != C:
         raise RuntimeError("`d_attr` must have shape [V, C] where C matches d_image.shape(3)")
+    acc = torch.empty(d_attr.shape[0] * C, dtype=torch.float64, device=d_attr.device)
     call("s2c_backward_dda_interpolate_attributes", B, H, W, C, ptr(rast_dda), ptr(d_image), edges.shape[0], ptr(edges),
-         d_attr.shape[0], ptr(d_attr), _stream(rast_dda))
+         d_attr.shape[0], ptr(d_attr), ptr(acc), _stream(rast_dda))
 
 
 # ---- bitsets (pystrns2cards.cpp:480-529) ---------------------------------------------

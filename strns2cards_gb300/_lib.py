@@ -49,9 +49,9 @@ SIGNATURES = {
     "s2c_msaa_resolve": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, vp, vp], c_i),
     "s2c_barycentric_derivatives": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, vp], c_i),
     "s2c_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp], c_i),
-    "s2c_backward_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp], c_i),
+    "s2c_backward_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp, vp], c_i),
     "s2c_dda_interpolate_attributes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp], c_i),
-    "s2c_backward_dda_interpolate_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp], c_i),
+    "s2c_backward_dda_interpolate_attributes": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, c_i, vp, vp, vp], c_i),
     "s2c_xor_popcount": ([c_i64, vp, vp, vp, vp], c_i),
     "s2c_cluster_iou_counts": ([c_i64, c_i, c_i, vp, vp, vp, vp, vp], c_i),
     "s2c_mark_discontinuity_edges": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, vp], c_i),

@@ -478,11 +478,21 @@ __global__ void __launch_bounds__(256) msaa_resolve_kernel(int S, int64_t npix, 
     }
 }
 
-// rasterize.cu:402-438: scatter-add of grad * b_i (float atomics, as the reference)
+// rasterize.cu:402-438: scatter-add of grad * b_i.  Acc = float: float atomics into d_attr,
+// as the reference.  Acc = double: each FP32 x FP32 product is exact in FP64 and is summed
+// there (FP64 L2 atomics into a caller accumulator); finish_acc64 rounds each sum once.
+template <typename Acc>
+__device__ __forceinline__ void acc_add(Acc* a, float g, float b);
+template <>
+__device__ __forceinline__ void acc_add<float>(float* a, float g, float b) { atomicAdd(a, __fmul_rn(g, b)); }
+template <>
+__device__ __forceinline__ void acc_add<double>(double* a, float g, float b) { atomicAdd(a, (double)g * (double)b); }
+
+template <typename Acc>
 __global__ void __launch_bounds__(256) interp_backward_kernel(int64_t npix, const float4* __restrict__ rast, int C,
                                                               const float* __restrict__ d_image,
                                                               const int* __restrict__ tri, int T, int V,
-                                                              float* __restrict__ d_attr) {
+                                                              Acc* __restrict__ d_attr) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
     const float4 r = rast[p];
@@ -493,10 +503,16 @@ __global__ void __launch_bounds__(256) interp_backward_kernel(int64_t npix, cons
     if ((unsigned)v0 >= (unsigned)V || (unsigned)v1 >= (unsigned)V || (unsigned)v2 >= (unsigned)V) return;
     for (int d = 0; d < C; ++d) {
         const float g = d_image[p * C + d];
-        atomicAdd(d_attr + (int64_t)C * v0 + d, __fmul_rn(g, b0));
-        atomicAdd(d_attr + (int64_t)C * v1 + d, __fmul_rn(g, b1));
-        atomicAdd(d_attr + (int64_t)C * v2 + d, __fmul_rn(g, b2));
+        acc_add<Acc>(d_attr + (int64_t)C * v0 + d, g, b0);
+        acc_add<Acc>(d_attr + (int64_t)C * v1 + d, g, b1);
+        acc_add<Acc>(d_attr + (int64_t)C * v2 + d, g, b2);
     }
+}
+
+// d_attr += round_to_float(acc): one rounding of each FP64 sum
+__global__ void __launch_bounds__(256) finish_acc64(int64_t n, const double* __restrict__ acc, float* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __fadd_rn(out[i], __double2float_rn(acc[i]));
 }
 
 // dda.cu:258-284
@@ -516,11 +532,12 @@ __global__ void __launch_bounds__(256) dda_interp_kernel(int64_t npix, const flo
         image[p * C + d] = __fmaf_rn(t1, __ldg(attr + (int64_t)C * ev.y + d), __fmul_rn(t0, __ldg(attr + (int64_t)C * ev.x + d)));
 }
 
-// dda.cu:300-327
+// dda.cu:300-327 (float or FP64 accumulation, as interp_backward_kernel)
+template <typename Acc>
 __global__ void __launch_bounds__(256) dda_interp_backward_kernel(int64_t npix, const float4* __restrict__ rast, int C,
                                                                   const float* __restrict__ d_image,
                                                                   const int2* __restrict__ edges, int E, int V,
-                                                                  float* __restrict__ d_attr) {
+                                                                  Acc* __restrict__ d_attr) {
     const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npix) return;
     const float4 r = rast[p];
@@ -531,8 +548,8 @@ __global__ void __launch_bounds__(256) dda_interp_backward_kernel(int64_t npix, 
     if ((unsigned)ev.x >= (unsigned)V || (unsigned)ev.y >= (unsigned)V) return;
     for (int d = 0; d < C; ++d) {
         const float g = d_image[p * C + d];
-        atomicAdd(d_attr + (int64_t)C * ev.x + d, __fmul_rn(g, t0));
-        atomicAdd(d_attr + (int64_t)C * ev.y + d, __fmul_rn(g, t1));
+        acc_add<Acc>(d_attr + (int64_t)C * ev.x + d, g, t0);
+        acc_add<Acc>(d_attr + (int64_t)C * ev.y + d, g, t1);
     }
 }
 
@@ -708,16 +725,30 @@ extern "C" s2c_status s2c_interpolate_triangle_attributes(int B, int H, int W, i
 
 extern "C" s2c_status s2c_backward_interpolate_triangle_attributes(int B, int H, int W, int C, const float* rast,
                                                                    const float* d_image, int T, const int32_t* tri,
-                                                                   int V, float* d_attr, s2c_stream stream) {
+                                                                   int V, float* d_attr, double* acc64,
+                                                                   s2c_stream stream) {
     S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && T >= 0,
                 "backward_interpolate_triangle_attributes: bad sizes");
     const int64_t npix = (int64_t)B * H * W;
     if (npix == 0 || C == 0) return S2C_OK;
     S2C_REQUIRE(rast && d_image && tri && d_attr && ((uintptr_t)rast & 15) == 0,
                 "backward_interpolate_triangle_attributes: bad pointer");
-    interp_backward_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(npix, (const float4*)rast, C, d_image,
-                                                                                  tri, T, V, d_attr);
+    S2C_REQUIRE(((uintptr_t)acc64 & 7) == 0, "backward_interpolate_triangle_attributes: misaligned accumulator");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!acc64) {
+        interp_backward_kernel<float><<<grid_for(npix, 256), 256, 0, st>>>(npix, (const float4*)rast, C, d_image, tri, T,
+                                                                            V, d_attr);
+        S2C_CHECK_LAUNCH("interp_backward_kernel");
+        return S2C_OK;
+    }
+    const int64_t n = (int64_t)V * C;
+    if (cudaError_t e = cudaMemsetAsync(acc64, 0, (size_t)n * sizeof(double), st))
+        return cuda_status(e, "backward_interpolate_triangle_attributes: clearing the accumulator");
+    interp_backward_kernel<double><<<grid_for(npix, 256), 256, 0, st>>>(npix, (const float4*)rast, C, d_image, tri, T, V,
+                                                                         acc64);
     S2C_CHECK_LAUNCH("interp_backward_kernel");
+    finish_acc64<<<grid_for(n, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(n, acc64, d_attr);
+    S2C_CHECK_LAUNCH("finish_acc64");
     return S2C_OK;
 }
 
@@ -737,16 +768,29 @@ extern "C" s2c_status s2c_dda_interpolate_attributes(int B, int H, int W, int C,
 
 extern "C" s2c_status s2c_backward_dda_interpolate_attributes(int B, int H, int W, int C, const float* rast,
                                                               const float* d_image, int E, const int32_t* edges, int V,
-                                                              float* d_attr, s2c_stream stream) {
+                                                              float* d_attr, double* acc64, s2c_stream stream) {
     S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && C >= 0 && V >= 0 && E >= 0,
                 "backward_dda_interpolate_attributes: bad sizes");
     const int64_t npix = (int64_t)B * H * W;
     if (npix == 0 || C == 0) return S2C_OK;
     S2C_REQUIRE(rast && d_image && edges && d_attr && ((uintptr_t)rast & 15) == 0 && ((uintptr_t)edges & 7) == 0,
                 "backward_dda_interpolate_attributes: bad pointer");
-    dda_interp_backward_kernel<<<grid_for(npix, 256), 256, 0, (cudaStream_t)stream>>>(
-        npix, (const float4*)rast, C, d_image, (const int2*)edges, E, V, d_attr);
+    S2C_REQUIRE(((uintptr_t)acc64 & 7) == 0, "backward_dda_interpolate_attributes: misaligned accumulator");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (!acc64) {
+        dda_interp_backward_kernel<float><<<grid_for(npix, 256), 256, 0, st>>>(
+            npix, (const float4*)rast, C, d_image, (const int2*)edges, E, V, d_attr);
+        S2C_CHECK_LAUNCH("dda_interp_backward_kernel");
+        return S2C_OK;
+    }
+    const int64_t n = (int64_t)V * C;
+    if (cudaError_t e = cudaMemsetAsync(acc64, 0, (size_t)n * sizeof(double), st))
+        return cuda_status(e, "backward_dda_interpolate_attributes: clearing the accumulator");
+    dda_interp_backward_kernel<double><<<grid_for(npix, 256), 256, 0, st>>>(
+        npix, (const float4*)rast, C, d_image, (const int2*)edges, E, V, acc64);
     S2C_CHECK_LAUNCH("dda_interp_backward_kernel");
+    finish_acc64<<<grid_for(n, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(n, acc64, d_attr);
+    S2C_CHECK_LAUNCH("finish_acc64");
     return S2C_OK;
 }
 

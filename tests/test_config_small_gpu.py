@@ -6,7 +6,7 @@ strands x 32 vertices (the generator), one orthographic 256x256 view, 64 cluster
 - card raster (rast = b0, b1, z, triangle id + 1) and the cards' cluster bitset: triangle
   ids, coverage and bits exact, b0 / b1 / z equal to the oracle's FP32 mirror;
 - attribute interpolation forward and backward with an N(0, 1) upstream image gradient
-  (seed 0): 1e-5 of the max-norm against FP64;
+  (seed 0): elementwise against FP64, |got - FP64| <= 1e-5 x max(|FP64|, sum|terms|);
 - antialias forward (XOR-popcount loss) exact and backward d_pos within 1e-5 elementwise
   (floor 1e-3 of the max-norm) of the FP64 oracle, the same non-zero pattern.
 """
@@ -15,6 +15,7 @@ import pytest
 import torch
 
 from oracle import oracle as O
+from parity import assert_rel
 
 pytestmark = pytest.mark.gpu
 
@@ -70,14 +71,14 @@ def test_small_config_card_raster_and_interpolation(scene):
     assert np.array_equal(rast[..., :3], ref[..., :3])
     attr = np.random.default_rng(0).normal(size=(cpos.shape[1], 3)).astype(np.float32)
     img = np_(s2c.interpolate_triangle_attributes(cu(rast), cu(attr), cu(tri)))
-    oimg = O.interpolate(rast, attr, tri)
-    assert np.abs(img - oimg).max() <= 1e-5 * max(np.abs(oimg).max(), 1e-30)
+    assert_rel(img, O.interpolate(rast, attr, tri), O.interpolate_mag(rast, attr, tri), 1e-5, "image")
     grad = torch.randn((1, H, W, 3), generator=torch.Generator().manual_seed(0)).numpy()
     a = cu(attr).requires_grad_(True)
     out = s2c.interpolate_triangle_attributes(cu(rast), a, cu(tri))
     out.backward(cu(grad))
-    og = O.interpolate_backward(rast, grad, tri, cpos.shape[1])
-    assert np.abs(np_(a.grad) - og).max() <= 1e-5 * max(np.abs(og).max(), 1e-30)
+    V = cpos.shape[1]
+    assert_rel(np_(a.grad), O.interpolate_backward(rast, grad, tri, V), O.interpolate_backward_mag(rast, grad, tri, V),
+               1e-5, "d_attr")
 
 
 def test_small_config_antialias(scene):
