@@ -196,7 +196,75 @@ def run_reference(args):
             "cpu_baseline": {"value": val, "unit": "Gseg/s", "cores": threads, "kind": "port",
                              "sample": "the full 4.95M-segment workload per step"},
             "e2e": {"value": val, "unit": "Gseg/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_forms:
+        line["reference_gpu"] = reference_gpu_numbers()
     print(json.dumps(line), flush=True)
+
+
+def reference_gpu_numbers(reps=5):
+    """The reference's own CUDA kernels (built unmodified from its sources into cubins by
+    oracle/build_ref.sh) on this GPU, for the headline op and the fitting iteration's two
+    main ops, called in the reference's op sequences; median ms of ``reps`` calls each.
+    None when there is no GPU or the cubins were not built."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        from oracle import refkern
+        if not refkern.available():
+            return None
+    except Exception as e:  # pragma: no cover - reported, not fatal to the CPU arm
+        return {"unavailable": str(e)}
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import synthetic as syn
+    rk = refkern.RefKernels()
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+    out = {}
+    pos_h, edges_h, e2c_h = make_inputs(0)
+    pos, edges, e2c = (torch.from_numpy(a).cuda() for a in (pos_h, edges_h, e2c_h))
+
+    def dda_ref():
+        (fp, fa), _ = rk.dda_compute_fragments(RES, RES, pos, edges)
+        return rk.cluster_mask_from_fragments(RES, RES, fp, fa, e2c, K)
+    ms = timed(dda_ref)
+    out["dda_cluster_bitset"] = {"ms": ms, "Gseg_per_s": edges_h.shape[0] / ms / 1e6,
+                                 "ops": "dda_compute_fragments + cluster_mask_from_fragments (reference kernels)"}
+    strands = syn.make_strands(NUM_STRANDS, NUM_VERTS, seed=0)
+    mvp = syn.ortho_cameras(strands, margin=0.3, num_views=1)
+    cards = syn.make_cards(strands, 0, 16, 4, num_cards=2048)
+    cpos = torch.from_numpy(syn.project(cards.verts, mvp)).cuda()
+    tri, t2c = torch.from_numpy(cards.tri).cuda(), torch.from_numpy(cards.tri2cluster).cuda()
+
+    def raster_ref():
+        (fp, fa) = rk.compute_fragments(RES, RES, cpos, tri)[0]
+        return rk.depth_test(1, RES, RES, fp, fa), rk.cluster_mask_from_fragments(RES, RES, fp, fa, t2c, K)
+    ms = timed(raster_ref)
+    out["card_raster"] = {"ms": ms, "Mtri_per_s": cards.tri.shape[0] / ms / 1e3,
+                          "ops": "compute_fragments + depth_test + cluster_mask_from_fragments, 2,048 cards "
+                                 "(262,144 triangles), 1024x1024, K=2048"}
+    bits = raster_ref()[1]
+    target = dda_ref()
+    e_h, e2t_h = s2c.build_edges_from_triangles(cards.tri)
+    ce2c = torch.from_numpy(cards.tri2cluster[e2t_h[:, 0]].astype(np.int32)).cuda()
+    cedges, e2t = torch.from_numpy(e_h).cuda(), torch.from_numpy(e2t_h).cuda()
+    ms = timed(lambda: rk.antialiased_loss_grad(bits, target, cpos, tri, cedges, e2t, ce2c, 7.0, 0.5))
+    out["antialias_backward"] = {"ms": ms, "Medge_per_s": e_h.shape[0] / ms / 1e3,
+                                 "ops": "mark_discontinuity_edges + compact + dda_compute_fragments + "
+                                        "backward_antialiased_cluster_bitset, the cards against the strands' bitset"}
+    out["gpu"] = torch.cuda.get_device_name(0)
+    return out
 
 
 def run_ours(args):
@@ -327,6 +395,15 @@ def run_ours(args):
                              "kernel": "s2c_dda_cluster_bitset (init, bin, tile scan, scatter, tile raster, fixup)"},
                 "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": LAUNCHES_PER_STEP * args.steps,
                 "wall_s": wall}
+        if ws == 1 and not args.no_forms:
+            # the chosen forms, after the headline's timed region: the batched fit of 256
+            # uneven clusters against their per-cluster call sequence, and the continuous-
+            # batching server on a short Poisson stream against serial plain calls
+            del work, flush, dins, douts, outs_p
+            torch.cuda.empty_cache()
+            line["batched"] = batched_numbers(steps=20, plain_iters=2, trials=2)
+            torch.cuda.empty_cache()
+            line["serving"] = serving_numbers(args.serving_jobs)
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -732,42 +809,42 @@ def wl_laplacian():
                 workload="10 Jacobi Laplacian steps (lambda 0.5) on 4,096 cards of 32x4 quads (165 vertices each)")
 
 
-def run_batched_fit(args):
-    """Batched cluster fit: 256 clusters (log-uniform 20..2000 strands x 64 vertices, seed 0),
-    local 128 x 512 frames, K = 1, one 32 x 4-quad card each; an iteration = coverage + card
-    raster + antialias backward + 10 Laplacian steps.  Metric: cluster-fit iterations per
-    second of the autotuned batched schedule; the per-cluster call sequence is timed beside."""
+def batched_numbers(steps, warmup=3, plain_iters=2, trials=3):
+    """Batched cluster fit (256 clusters, log-uniform 20..2000 strands x 64 vertices, seed 0;
+    local 128 x 512 frames, K = 1, one 32 x 4-quad card each): cluster-fit iterations per
+    second of the autotuned schedule, the per-cluster call sequence timed beside it, and end
+    to end with positions copied in from pinned host memory and cards copied out."""
     import torch
     from strns2cards_gb300.batched import BatchedClusterFit, FitSchedule, synthetic_clusters
     batch = synthetic_clusters()
     C = batch.card_pos.shape[0]
     fit = BatchedClusterFit(batch)
-    sched = FitSchedule(fit, trials=3)
-    for _ in range(max(args.warmup, 3)):
+    sched = FitSchedule(fit, trials=trials)
+    for _ in range(max(warmup, 3)):
         fit.step()
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(0) as clk:
         a.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             fit.step()
         b.record(stream)
         torch.cuda.synchronize()
     t = a.elapsed_time(b) / 1e3
-    value = C * args.steps / t
+    value = C * steps / t
     # the per-cluster call sequence (the reference's way of fitting), a few iterations
     plain = BatchedClusterFit(batch)
     plain.prepare_plain()
     plain.plain_iteration()
     torch.cuda.synchronize()
-    k = 2
     a.record(stream)
-    for _ in range(k):
+    for _ in range(plain_iters):
         plain.plain_iteration()
     b.record(stream)
     torch.cuda.synchronize()
-    plain_rate = C * k / (a.elapsed_time(b) / 1e3)
+    plain_rate = C * plain_iters / (a.elapsed_time(b) / 1e3)
+    del plain
     # end to end: card and strand positions in from pinned host memory, cards out
     sp = torch.from_numpy(batch.strand_pos).pin_memory()
     cp = torch.from_numpy(batch.card_pos).pin_memory()
@@ -789,30 +866,41 @@ def run_batched_fit(args):
     b.record(stream)
     torch.cuda.synchronize()
     e2e = C * 3 / (a.elapsed_time(b) / 1e3)
-    line = {"metric": "cluster-fit iterations per second (batched, autotuned schedule)", "value": value,
+    return dict(clusters=C, value=value, unit="cluster-iter/s", ms_per_iteration=1e3 * t / steps, steps=steps,
+                schedule=sched.best, schedule_ms=sched.results, tuned=getattr(sched, "table", None),
+                plain_per_cluster_calls=plain_rate, batched_over_plain=value / plain_rate, e2e=e2e,
+                h2d_bytes_per_step=sp.nbytes + cp.nbytes, d2h_bytes_per_step=out.nbytes,
+                strand_segments=int(batch.edge_ids.shape[0]), clocks=clk.summary())
+
+
+def run_batched_fit(args):
+    """Batched cluster fit on its own line (``--workload batched_fit``)."""
+    r = batched_numbers(args.steps, args.warmup)
+    C = r["clusters"]
+    line = {"metric": "cluster-fit iterations per second (batched, autotuned schedule)", "value": r["value"],
             "unit": "cluster-iter/s", "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3),
-            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": r["ms_per_iteration"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{C} clusters (log-uniform 20..2000 strands x 64 verts, seed 0), 128x512 local "
                                    "frames, K=1, one 32x4-quad card each; iteration = fused DDA coverage + fused "
                                    "card raster + fused antialias backward + gradient step + 10 Laplacian steps",
-                       "schedule": sched.best, "schedule_ms": sched.results,
-                       "plain_per_cluster_calls": {"value": plain_rate, "unit": "cluster-iter/s"},
-                       "batched_over_plain": value / plain_rate, "strand_segments": int(batch.edge_ids.shape[0])},
-            "e2e": {"value": e2e, "unit": "cluster-iter/s", "h2d_bytes_per_step": sp.nbytes + cp.nbytes,
-                    "d2h_bytes_per_step": out.nbytes},
-            "roofline": None, "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": None}
+                       "schedule": r["schedule"], "schedule_ms": r["schedule_ms"], "tuned": r["tuned"],
+                       "plain_per_cluster_calls": {"value": r["plain_per_cluster_calls"], "unit": "cluster-iter/s"},
+                       "batched_over_plain": r["batched_over_plain"], "strand_segments": r["strand_segments"]},
+            "e2e": {"value": r["e2e"], "unit": "cluster-iter/s", "h2d_bytes_per_step": r["h2d_bytes_per_step"],
+                    "d2h_bytes_per_step": r["d2h_bytes_per_step"]},
+            "roofline": None, "cpu_baseline": None, "clocks": r["clocks"], "gpu_launches": None}
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args):
+def serving_numbers(n_jobs):
     """Continuous-batching server on a Poisson request stream (20 req/s, seed 1) of fitting
     jobs (strands log-uniform 5k..200k, V in {32, 64, 128}, resolution in {512, 1024, 2048},
     K in {256, 1024, 4096}, 50 iterations each), HBM budget 150 GB; the same stream served
     one job at a time with plain calls is timed beside it."""
     import torch
     from strns2cards_gb300.serving import poisson_stream, serve, serve_serial
-    n = max(args.steps, 4)
+    n = max(n_jobs, 4)
     reqs = poisson_stream(n, rate=20.0, seed=1)
     warm = poisson_stream(2, rate=20.0, seed=2, scale=0.05, iterations=3)
     serve(warm, 150 << 30)
@@ -829,21 +917,32 @@ def run_serving(args):
     lat_s = np.array([r.latency for r in ser])
     h2d = sum(r.strand_pos.nbytes + r.strand_edges.nbytes + r.strand_e2c.nbytes + r.card_pos.nbytes +
               r.card_tri.nbytes + r.card_t2c.nbytes for r in reqs)
-    line = {"metric": "served fitting jobs per second (continuous batching)", "value": n / wall, "unit": "jobs/s",
-            "n_gpus": 1, "steps": n, "warmup": 2, "ms_per_step": 1e3 * wall / n, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+    return dict(jobs=n, jobs_per_s=n / wall, iterations_per_s=iters / wall, wall_s=wall,
+                latency_p50_s=float(np.percentile(lat, 50)), latency_p99_s=float(np.percentile(lat, 99)),
+                serial_plain={"jobs_per_s": n / wall_s, "iterations_per_s": iters / wall_s,
+                              "latency_p50_s": float(np.percentile(lat_s, 50)),
+                              "latency_p99_s": float(np.percentile(lat_s, 99))},
+                served_over_serial_iterations=(iters / wall) / (iters / wall_s),
+                h2d_bytes_per_job=h2d // n, d2h_bytes_per_job=sum(r.card_pos.nbytes for r in reqs) // n,
+                clocks=clk.summary())
+
+
+def run_serving(args):
+    """The served form on its own line (``--workload serving``)."""
+    r = serving_numbers(args.steps)
+    n = r["jobs"]
+    line = {"metric": "served fitting jobs per second (continuous batching)", "value": r["jobs_per_s"],
+            "unit": "jobs/s", "n_gpus": 1, "steps": n, "warmup": 2, "ms_per_step": 1e3 * r["wall_s"] / n,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"{n} Poisson requests (20/s, seed 1): strands log-uniform 5k..200k, V in "
                                    "{32,64,128}, res in {512,1024,2048}, K in {256,1024,4096}, 50 iterations of the "
                                    "full-size pipeline each; HBM budget 150 GB",
-                       "iterations_per_s": iters / wall, "latency_p50_s": float(np.percentile(lat, 50)),
-                       "latency_p99_s": float(np.percentile(lat, 99)),
-                       "serial_plain": {"jobs_per_s": n / wall_s, "iterations_per_s": iters / wall_s,
-                                        "latency_p50_s": float(np.percentile(lat_s, 50)),
-                                        "latency_p99_s": float(np.percentile(lat_s, 99))},
-                       "served_over_serial_iterations": (iters / wall) / (iters / wall_s)},
-            "e2e": {"value": n / wall, "unit": "jobs/s", "h2d_bytes_per_step": h2d // n,
-                    "d2h_bytes_per_step": sum(r.card_pos.nbytes for r in reqs) // n},
-            "roofline": None, "cpu_baseline": None, "clocks": clk.summary(), "gpu_launches": None}
+                       "iterations_per_s": r["iterations_per_s"], "latency_p50_s": r["latency_p50_s"],
+                       "latency_p99_s": r["latency_p99_s"], "serial_plain": r["serial_plain"],
+                       "served_over_serial_iterations": r["served_over_serial_iterations"]},
+            "e2e": {"value": r["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": r["h2d_bytes_per_job"],
+                    "d2h_bytes_per_step": r["d2h_bytes_per_job"]},
+            "roofline": None, "cpu_baseline": None, "clocks": r["clocks"], "gpu_launches": None}
     print(json.dumps(line), flush=True)
 
 
@@ -1112,6 +1211,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched / served forms (ours) and the reference-kernel timings (reference)")
+    ap.add_argument("--serving-jobs", type=int, default=40, help="requests in the served form's stream")
     ap.add_argument("--workload", choices=["dda_bitset", "batched_fit", "serving"] + sorted(WORKLOADS),
                     default="dda_bitset",
                     help="dda_bitset (default) is the headline; the others time the remaining rows")

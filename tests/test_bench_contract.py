@@ -35,6 +35,9 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # the reference's own kernels on the GPU are timed beside it where a GPU is present
+    rg = d["reference_gpu"]
+    assert rg is None or ("unavailable" in rg) or rg["dda_cluster_bitset"]["ms"] > 0
 
 
 def test_reference_arm_other_ranks_exit_quietly():
@@ -47,7 +50,8 @@ def test_reference_arm_other_ranks_exit_quietly():
 def test_headline_arm_prints_one_contract_line():
     """The headline arm on the GPU: roofline, cpu_baseline (skipped here), clocks, e2e with
     the copied bytes and the launch count."""
-    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--steps", "3", "--warmup", "3", "--no-cpu-baseline"]
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--steps", "3", "--warmup", "3", "--no-cpu-baseline",
+           "--serving-jobs", "6"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -61,3 +65,10 @@ def test_headline_arm_prints_one_contract_line():
     assert e2e["value"] > 0 and e2e["h2d_bytes_per_step"] > 0 and e2e["d2h_bytes_per_step"] == 1024 * 1024 * 64 * 4
     assert d["gpu_launches"] == 6 * 3
     assert d["clocks"] is None or set(d["clocks"]) >= {"sm_mhz", "sm_max_mhz", "reasons"}  # None: no nvidia-smi
+    # the forms, measured after the headline's timed region
+    b = d["batched"]
+    assert b["value"] > 0 and b["plain_per_cluster_calls"] > 0 and b["clusters"] == 256
+    assert b["batched_over_plain"] == b["value"] / b["plain_per_cluster_calls"]
+    sv = d["serving"]
+    assert sv["jobs"] == 6 and sv["jobs_per_s"] > 0 and sv["latency_p99_s"] >= sv["latency_p50_s"] > 0
+    assert sv["serial_plain"]["jobs_per_s"] > 0
