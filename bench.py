@@ -401,7 +401,12 @@ def run_ours(args):
             # batching server on a short Poisson stream against serial plain calls
             del work, flush, dins, douts, outs_p
             torch.cuda.empty_cache()
-            line["batched"] = batched_numbers(steps=20, plain_iters=2, trials=2)
+            bt = batched_numbers(steps=20, plain_iters=2, trials=2)
+            ms = bt.pop("schedule_ms")
+            bt["candidates_timed"] = len(ms)
+            bt["schedule_ms_fastest5"] = dict(sorted(ms.items(), key=lambda kv: kv[1])[:5])
+            bt["schedule_ms_slowest"] = max(ms.values())
+            line["batched"] = bt
             torch.cuda.empty_cache()
             line["serving"] = serving_numbers(args.serving_jobs)
         print(json.dumps(line), flush=True)
@@ -819,7 +824,7 @@ def batched_numbers(steps, warmup=3, plain_iters=2, trials=3):
     batch = synthetic_clusters()
     C = batch.card_pos.shape[0]
     fit = BatchedClusterFit(batch)
-    sched = FitSchedule(fit, trials=trials)
+    sched = FitSchedule(fit, trials=trials, search=True)
     for _ in range(max(warmup, 3)):
         fit.step()
     torch.cuda.synchronize()
@@ -849,9 +854,7 @@ def batched_numbers(steps, warmup=3, plain_iters=2, trials=3):
     sp = torch.from_numpy(batch.strand_pos).pin_memory()
     cp = torch.from_numpy(batch.card_pos).pin_memory()
     out = torch.empty(cp.shape, dtype=torch.float32).pin_memory()
-    fit.mode = "graph" if sched.best.startswith("graph") else sched.best
-    if fit.mode == "graph":
-        fit.capture(two_streams=sched.best == "graph2")
+    # the schedule stays applied (its graph, or the eager sequence)
 
     def e2e_step():
         fit.spos.copy_(sp, non_blocking=True)
@@ -867,7 +870,8 @@ def batched_numbers(steps, warmup=3, plain_iters=2, trials=3):
     torch.cuda.synchronize()
     e2e = C * 3 / (a.elapsed_time(b) / 1e3)
     return dict(clusters=C, value=value, unit="cluster-iter/s", ms_per_iteration=1e3 * t / steps, steps=steps,
-                schedule=sched.best, schedule_ms=sched.results, tuned=getattr(sched, "table", None),
+                schedule=sched.best, schedule_params=sched.best_params, schedule_ms=sched.results,
+                tuned_parameters=list(FitSchedule.SPACE),
                 plain_per_cluster_calls=plain_rate, batched_over_plain=value / plain_rate, e2e=e2e,
                 h2d_bytes_per_step=sp.nbytes + cp.nbytes, d2h_bytes_per_step=out.nbytes,
                 strand_segments=int(batch.edge_ids.shape[0]), clocks=clk.summary())
@@ -884,7 +888,8 @@ def run_batched_fit(args):
             "config": {"workload": f"{C} clusters (log-uniform 20..2000 strands x 64 verts, seed 0), 128x512 local "
                                    "frames, K=1, one 32x4-quad card each; iteration = fused DDA coverage + fused "
                                    "card raster + fused antialias backward + gradient step + 10 Laplacian steps",
-                       "schedule": r["schedule"], "schedule_ms": r["schedule_ms"], "tuned": r["tuned"],
+                       "schedule": r["schedule"], "schedule_params": r["schedule_params"],
+                       "schedule_ms": r["schedule_ms"], "tuned_parameters": r["tuned_parameters"],
                        "plain_per_cluster_calls": {"value": r["plain_per_cluster_calls"], "unit": "cluster-iter/s"},
                        "batched_over_plain": r["batched_over_plain"], "strand_segments": r["strand_segments"]},
             "e2e": {"value": r["e2e"], "unit": "cluster-iter/s", "h2d_bytes_per_step": r["h2d_bytes_per_step"],

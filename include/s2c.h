@@ -119,6 +119,36 @@ S2C_API s2c_status s2c_dda_cluster_bitset_noalloc(int64_t num_prims, const int32
                                                   int W, int B, int V, const float* pos, int E,
                                                   const int32_t* edges, const int32_t* prim2cluster,
                                                   int S, int32_t* bitset, s2c_stream stream);
+/* new (no single reference call; one iteration of the per-cluster fitting loop of
+ * 3_fitting.py:381-406 for every cluster at once, in one persistent launch).  C clusters,
+ * each framed at H x W with one cluster per view: strands strand_pos (C, Vs, 4) with a
+ * shared edge list strand_edges (Es, 2) and edge_ids[i] = c * Es + e grouped by cluster,
+ * cluster c owning edge_ids[cluster_offsets[c] .. cluster_offsets[c + 1]); cards card_pos
+ * (C, Vc, 4), updated in place, sharing card_tri (Tc, 3), card_edges / card_edge2tri (Ec, 2)
+ * and the Laplacian neighbour CSR of one card (lap_offsets (Vc + 1), lap_adj (nadj)).
+ * Per cluster: the strands' DDA coverage (exact, as dda_compute_fragments +
+ * cluster_mask_from_fragments), the card raster's coverage (exact), the antialiased-bitset
+ * gradient d_pos (FP64 sums), x, y -= d_pos * (step_scale / max |d_pos.xy|), then
+ * laplacian_steps Jacobi steps p -= lam (p - mean of neighbours).  items (n_items, 2) lists
+ * (cluster, chunk) work items in processing order with chunk segments each and
+ * chunks_per_cluster (C) their counts; threads (128/256/512/1024), ctas_per_sm and aa_warp
+ * (one warp rather than one thread per antialias fragment) shape the launch.  Limits:
+ * H * ceil(W / 32) <= 16384, Vc <= 2048, Ec <= 8192.  The workspace is cleared on the
+ * stream by each call; calls sharing one workspace must not overlap. */
+S2C_API size_t s2c_fit_smem_bytes(int H, int W, int Vc, int Ec, int nadj);
+S2C_API size_t s2c_fit_workspace_size(int C, int H, int W);
+S2C_API s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float* strand_pos, int Es,
+                                     const int32_t* strand_edges, const int32_t* edge_ids,
+                                     const int32_t* cluster_offsets, int Vc, float* card_pos,
+                                     int Tc, const int32_t* card_tri, int Ec,
+                                     const int32_t* card_edges, const int32_t* card_edge2tri,
+                                     const int32_t* lap_offsets, const int32_t* lap_adj, int nadj,
+                                     const int32_t* items, int n_items, int chunk,
+                                     const int32_t* chunks_per_cluster, float step_scale, float lam,
+                                     int laplacian_steps, float kernel_radius, float rho,
+                                     int threads, int ctas_per_sm, int aa_warp, void* workspace,
+                                     size_t workspace_bytes, s2c_stream stream);
+
 /* after a call on the same stream (synchronise first): how many primitives took the
  * global-atomic fallback because the workspace or a tile's record list was full */
 S2C_API s2c_status s2c_dda_cluster_bitset_stats(const void* workspace, size_t workspace_bytes,

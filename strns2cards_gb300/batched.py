@@ -8,19 +8,33 @@ clusters are the views ``b`` of single launches --
 * strands: vertices padded per cluster to ``(C, Vmax, 4)``; each cluster's own segments are
   selected by ``edge_ids = b * E + e``, so padding is never read;
 * cards: ``(C, Vc, 4)`` with one shared grid topology;
-* one iteration = target coverage (fused DDA), card raster (fused), antialiased-bitset
-  gradient (fused), a gradient step on the card vertices, ``laplacian_steps`` Jacobi
-  Laplacian steps -- five sync-free launches groups, captured in one CUDA graph.
+* one iteration = target coverage (DDA), card raster, antialiased-bitset gradient, a
+  gradient step on the card vertices and ``laplacian_steps`` Jacobi Laplacian steps.
 
-``FitSchedule`` is the autotuner: it times the eager launch sequence, the single-stream
-graph and a two-stream graph (target coverage overlapped with the card raster) on the
-first iterations and keeps the fastest.  ``plain_iteration`` runs the same work as one
-call sequence per cluster, the per-call path this batching replaces.
+Two ways to run an iteration:
+
+* ``persistent`` (``s2c_fit_iteration``): one launch.  CTAs take (cluster, segment chunk)
+  items from a queue, largest clusters first, rasterise their strand segments into a
+  one-bit target plane in shared memory, and the CTA that completes a cluster's coverage
+  runs the rest of that cluster's iteration in shared memory;
+* the launch sequence over all clusters (fused DDA -> bitset, fused card raster into
+  cluster planes, antialias backward from planes, the step, the Laplacian), eager or as a
+  CUDA graph, on one or two streams.
+
+``FitSchedule`` is the autotuner: on the first iterations it times the persistent launch
+over its parameters -- segments per coverage chunk (the segment-bin size), threads per CTA,
+CTAs per SM, and threads per antialias fragment (one thread, or a warp over the window
+rows) -- and the launch sequences, keeps the fastest, and caches the choice in a JSON file
+keyed by the problem's shape class.  ``plain_iteration`` runs the same work as one call
+sequence per cluster, the per-call path this batching replaces.
 """
 from __future__ import annotations
 
+import json
+import math
+import os
 from dataclasses import dataclass
-from typing import List
+from typing import Dict, List, Optional
 
 import numpy as np
 import torch
@@ -120,6 +134,17 @@ class BatchedClusterFit:
         self.side = torch.cuda.Stream(device=dev)
         self.graph = None
         self.mode = "eager"
+        # the persistent launch: per-cluster segment ranges of edge_ids (grouped by cluster)
+        E = batch.strand_edges.shape[0]
+        owner = batch.edge_ids.astype(np.int64) // max(E, 1)
+        if owner.size and np.any(np.diff(owner) < 0):
+            raise ValueError("BatchedClusterFit: edge_ids must be grouped by cluster (b * E + e, b non-decreasing).")
+        self.seg_counts = np.bincount(owner, minlength=C).astype(np.int64)[:C]
+        self.coff = t(np.concatenate([[0], np.cumsum(self.seg_counts)]).astype(np.int32))
+        self.ws_fit = torch.empty(L.s2c_fit_workspace_size(C, H, W), dtype=torch.uint8, device=dev)
+        self.step_scale = float(np.float32(2.0 * self.lr / max(H, W)))
+        self.params = dict(chunk=8192, threads=256, ctas_per_sm=2, aa_warp=0)
+        self._items: Dict[int, tuple] = {}
 
     # -- the five parts of an iteration --
     def _coverage(self):
@@ -145,6 +170,39 @@ class BatchedClusterFit:
         self.lap(self.xyz, self.lam, self.nlap, out=self.xyz)
         self.cpos[..., :3].copy_(self.xyz.view(self.C, -1, 3))
 
+    # -- the persistent launch --
+    def items(self, chunk: int):
+        """(cluster, chunk) work items, largest clusters first, and chunks per cluster."""
+        if chunk not in self._items:
+            n = np.maximum(1, -(-self.seg_counts // chunk)).astype(np.int32)
+            order = np.argsort(-self.seg_counts, kind="stable")
+            it = np.array([(c, k) for c in order for k in range(int(n[c]))], np.int32).reshape(-1, 2)
+            dev = self.cpos.device
+            self._items[chunk] = (torch.from_numpy(it).to(dev), torch.from_numpy(n).to(dev), int(it.shape[0]))
+        return self._items[chunk]
+
+    def persistent_step(self, params: Optional[dict] = None):
+        """One iteration for every cluster in one launch (``s2c_fit_iteration``)."""
+        p = dict(self.params, **(params or {}))
+        items, nch, n_items = self.items(int(p["chunk"]))
+        lap = self.lap
+        _lib.call("s2c_fit_iteration", self.C, self.H, self.W, self.spos.shape[1], _lib.ptr(self.spos),
+                  self.sedges.shape[0], _lib.ptr(self.sedges), _lib.ptr(self.edge_ids), _lib.ptr(self.coff),
+                  self.cpos.shape[1], _lib.ptr(self.cpos), self.ctri.shape[0], _lib.ptr(self.ctri),
+                  self.cedges.shape[0], _lib.ptr(self.cedges), _lib.ptr(self.ce2t), _lib.ptr(lap.offsets),
+                  _lib.ptr(lap.adj), lap.num_adj, _lib.ptr(items), n_items, int(p["chunk"]), _lib.ptr(nch),
+                  self.step_scale, self.lam, self.nlap, self.kr, self.rho, int(p["threads"]), int(p["ctas_per_sm"]),
+                  int(p["aa_warp"]), _lib.ptr(self.ws_fit), self.ws_fit.numel(), _lib.stream_of(self.cpos))
+
+    def shape_key(self) -> str:
+        """Shape class of the problem for the tuning cache: frame, card, cluster count and the
+        (log2-bucketed) total and largest cluster segment counts, and the GPU's SM count."""
+        tot = int(self.seg_counts.sum())
+        mx = int(self.seg_counts.max()) if self.seg_counts.size else 0
+        sms = torch.cuda.get_device_properties(self.cpos.device).multi_processor_count
+        return (f"C{self.C}_H{self.H}_W{self.W}_Vc{self.cpos.shape[1]}_Ec{self.cedges.shape[0]}_"
+                f"seg2^{int(math.log2(max(tot, 1)))}_max2^{int(math.log2(max(mx, 1)))}_sm{sms}")
+
     def eager_step(self, two_streams: bool = False):
         if two_streams:
             cur = torch.cuda.current_stream()
@@ -158,22 +216,25 @@ class BatchedClusterFit:
             self._raster()
         self._update()
 
-    def capture(self, two_streams: bool = False):
+    def capture(self, two_streams: bool = False, persistent: bool = False):
         """Capture one iteration in a CUDA graph (after a warm-up on the side stream)."""
+        body = self.persistent_step if persistent else (lambda: self.eager_step(two_streams))
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):
-            self.eager_step(two_streams)
+            body()
         torch.cuda.current_stream().wait_stream(s)
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            self.eager_step(two_streams)
+            body()
         self.graph = g
         return g
 
     def step(self):
-        if self.mode.startswith("graph"):
+        if self.mode.startswith("graph") or self.mode == "persistent_graph":
             self.graph.replay()
+        elif self.mode == "persistent":
+            self.persistent_step()
         else:
             self.eager_step(self.mode == "eager2")
 
@@ -203,32 +264,121 @@ class BatchedClusterFit:
                            for c in range(self.C)]
 
 
-class FitSchedule:
-    """Autotuner over launch schedules of ``BatchedClusterFit.step``: eager, eager on two
-    streams, graph, graph on two streams.  Each is timed over ``trials`` iterations (CUDA
-    events) and the fastest is kept; the choice and timings are in ``self.results``."""
+def default_tuning_cache() -> str:
+    return os.environ.get("S2C_TUNING_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "strns2cards_gb300", "fit_tuning.json"))
 
-    def __init__(self, fit: BatchedClusterFit, trials: int = 5):
+
+class FitSchedule:
+    """Autotuner of ``BatchedClusterFit.step``.
+
+    Candidates: the persistent launch over ``SPACE`` (segments per coverage chunk, threads
+    per CTA, CTAs per SM, one thread or one warp per antialias fragment) and, with
+    ``launch_sequences``, the launch sequence eager / eager on two streams / as a graph / as
+    a two-stream graph.  Each is timed over ``trials`` iterations (CUDA events, one warm-up
+    iteration first); the card positions are restored afterwards.  The fastest is applied
+    (the persistent one then replayed from a CUDA graph) and stored in the JSON cache under
+    ``fit.shape_key()``; a later schedule for the same shape class reads it instead of
+    searching (``search=True`` searches regardless).  ``self.table`` lists every candidate
+    with its time (ms per iteration)."""
+
+    SPACE = dict(chunk=(2048, 4096, 8192, 16384, 32768), threads=(256, 512), ctas_per_sm=(1, 2, 4), aa_warp=(0, 1))
+
+    def __init__(self, fit: BatchedClusterFit, trials: int = 3, cache: Optional[str] = None, search: bool = False,
+                 launch_sequences: bool = True):
         self.fit = fit
-        self.results = {}
+        self.key = fit.shape_key()
+        self.cache = default_tuning_cache() if cache is None else cache
+        self.table: List[dict] = []
+        self.from_cache = False
+        stored = None if search else self._load().get(self.key)
         snap = fit.cpos.clone()
-        graphs = {}
-        for mode in ("eager", "eager2", "graph", "graph2"):
-            if mode.startswith("graph"):
-                graphs[mode] = fit.capture(two_streams=mode == "graph2")
-            fit.mode = mode
-            fit.graph = graphs.get(mode)
-            fit.step()
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record()
-            for _ in range(trials):
-                fit.step()
-            b.record()
-            torch.cuda.synchronize()
-            self.results[mode] = a.elapsed_time(b) / trials
+        if stored:
+            self.table = stored["table"]
+            best = stored["best"]
+            self.from_cache = True
+        else:
+            best = self._search(trials, launch_sequences)
+        self._apply(best)            # (a graph capture runs one warm-up iteration)
         fit.cpos.copy_(snap)
-        best = min(self.results, key=self.results.get)
-        fit.mode = best
-        fit.graph = graphs.get(best)
-        self.best = best
+        self.best = best["mode"]
+        self.best_params = best.get("params")
+        self.results = {r["name"]: r["ms"] for r in self.table}
+        if not stored:
+            self._save(best)
+
+    def _time(self, body, trials):
+        body()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(trials):
+            body()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / trials
+
+    def _search(self, trials, launch_sequences):
+        fit = self.fit
+        best = None
+        keys = list(self.SPACE)
+        for combo in _product([self.SPACE[k] for k in keys]):
+            params = dict(zip(keys, combo))
+            ms = self._time(lambda: fit.persistent_step(params), trials)
+            name = "persistent " + " ".join(f"{k}={v}" for k, v in params.items())
+            self.table.append({"name": name, "mode": "persistent", "params": params, "ms": ms})
+            if best is None or ms < best["ms"]:
+                best = {"mode": "persistent", "params": params, "ms": ms}
+        if launch_sequences:
+            for mode in ("eager", "eager2", "graph", "graph2"):
+                if mode.startswith("graph"):
+                    fit.capture(two_streams=mode == "graph2")
+                    body = fit.graph.replay
+                else:
+                    body = (lambda m=mode: fit.eager_step(m == "eager2"))
+                ms = self._time(body, trials)
+                self.table.append({"name": mode, "mode": mode, "ms": ms})
+                if ms < best["ms"]:
+                    best = {"mode": mode, "ms": ms}
+        return best
+
+    def _apply(self, best):
+        fit = self.fit
+        mode = best["mode"]
+        if mode == "persistent":
+            fit.params = dict(best["params"])
+            fit.capture(persistent=True)
+            fit.mode = "persistent_graph"
+        elif mode.startswith("graph"):
+            fit.capture(two_streams=mode == "graph2")
+            fit.mode = mode
+        else:
+            fit.mode = mode
+
+    def _load(self) -> dict:
+        try:
+            with open(self.cache) as f:
+                return json.load(f)
+        except (OSError, ValueError):
+            return {}
+
+    def _save(self, best):
+        try:
+            data = self._load()
+            data[self.key] = {"best": best, "table": self.table}
+            os.makedirs(os.path.dirname(self.cache) or ".", exist_ok=True)
+            tmp = self.cache + ".tmp"
+            with open(tmp, "w") as f:
+                json.dump(data, f, indent=1)
+            os.replace(tmp, self.cache)
+        except OSError:
+            pass   # an unwritable cache only costs a search next time
+
+
+def _product(lists):
+    if not lists:
+        yield ()
+        return
+    for x in lists[0]:
+        for rest in _product(lists[1:]):
+            yield (x,) + rest

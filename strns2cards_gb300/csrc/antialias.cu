@@ -10,6 +10,7 @@
 //   the reference; the weights use expf and the window sum is accumulated in FP64.
 #include <algorithm>
 
+#include "aa.cuh"
 #include "common.cuh"
 #include "scan.cuh"
 
@@ -24,43 +25,15 @@ struct Mesh {
     FastDiv divE;
 };
 
-__device__ __forceinline__ int third_vertex(const int* __restrict__ tri, int t, int v0, int v1) {
-    const int i0 = __ldg(tri + 3 * t), i1 = __ldg(tri + 3 * t + 1), i2 = __ldg(tri + 3 * t + 2);
-    return (i0 != v0 && i0 != v1) ? i0 : (i1 != v0 && i1 != v1) ? i1 : (i2 != v0 && i2 != v1) ? i2 : -1;
-}
+// mark_edge_t for edge e of view b of a mesh in global memory
+struct GlobalPos {
+    const float4* __restrict__ p;
+    __device__ __forceinline__ float4 operator()(int v) const { return __ldg(p + v); }
+};
 
-// antialias.cu:29-35 without the final multiply: (1 + x/w, 1 - y/w)
-__device__ __forceinline__ float2 ndc_a(float4 p) {
-    return make_float2(__fadd_rn(1.f, __fdiv_rn(p.x, p.w)), __fsub_rn(1.f, __fdiv_rn(p.y, p.w)));
-}
-
-// antialias.cu:38-94 for edge e of view b: 0 = zero-length edge (no normal), 1 = normal
-// only, 2 = silhouette or boundary edge (marked) with its oriented normal
 __device__ __forceinline__ int mark_edge(int H, int W, const Mesh& M, int b, int e, float2& nrm) {
-    const int2 ev = __ldg(M.edges + e);
-    if ((unsigned)ev.x >= (unsigned)M.V || (unsigned)ev.y >= (unsigned)M.V) return 0;
-    const float4* pb = M.pos4 + (int64_t)b * M.V;
-    const float hh = __fmul_rn((float)H, 0.5f), hw = __fmul_rn((float)W, 0.5f);
-    const float2 a0 = ndc_a(__ldg(pb + ev.x)), a1 = ndc_a(__ldg(pb + ev.y));
-    const float x0 = __fmul_rn(hw, a0.x), y0 = __fmul_rn(hh, a0.y);
-    const float dx = __fmaf_rn(hw, a1.x, -x0), dy = __fmaf_rn(hh, a1.y, -y0);
-    const float len = __fsqrt_rn(__fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-    if (len == 0.f) return 0;
-    const float nx = __fdiv_rn(-dy, len), ny = __fdiv_rn(dx, len);
-    float d[2] = {0.f, 0.f};
-    const int2 tt = __ldg(M.e2t + e);
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        const int t = i ? tt.y : tt.x;
-        if (t < 0 || t >= M.T) continue;
-        const int v2 = third_vertex(M.tri, t, ev.x, ev.y);
-        if ((unsigned)v2 >= (unsigned)M.V) continue;  // degenerate triangle (the reference reads out of bounds)
-        const float2 a2 = ndc_a(__ldg(pb + v2));
-        d[i] = __fmaf_rn(nx, __fmaf_rn(hw, a2.x, -x0), __fmul_rn(ny, __fmaf_rn(hh, a2.y, -y0)));
-    }
-    const float sign = __fmul_rn(2.f, __fsub_rn(0.5f, (float)(d[0] > 0.f || d[1] > 0.f)));
-    nrm = make_float2(__fmul_rn(sign, nx), __fmul_rn(sign, ny));
-    return __fmul_rn(d[0], d[1]) >= 0.f ? 2 : 1;
+    return mark_edge_t(H, W, __ldg(M.edges + e), __ldg(M.e2t + e), M.tri, M.T, M.V, GlobalPos{M.pos4 + (int64_t)b * M.V},
+                       nrm);
 }
 
 __global__ void __launch_bounds__(256) mark_edges_kernel(int H, int W, int B, Mesh M, int32_t* __restrict__ prim_ids,
@@ -94,35 +67,6 @@ struct AAArgs {
     int WQ;
     float kr, rho;
 };
-
-// Compensated FP32 sums (no FP64 arithmetic on the SMs: GB300's FP64 rate is a small
-// fraction of its FP32 rate).  kahan_add: running (sum, comp); two_sum_merge: error-free
-// merge of two compensated sums (Knuth's 2Sum on the leading parts).
-__device__ __forceinline__ void kahan_add(float& sum, float& comp, float v) {
-    const float y = __fsub_rn(v, comp);
-    const float t = __fadd_rn(sum, y);
-    comp = __fsub_rn(__fsub_rn(t, sum), y);
-    sum = t;
-}
-
-__device__ __forceinline__ void two_sum_merge(float& hi, float& lo, float ohi, float olo) {
-    const float s = __fadd_rn(hi, ohi);
-    const float bb = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(ohi, bb));
-    hi = s;
-    lo = __fadd_rn(__fadd_rn(lo, olo), err);
-}
-
-// warp-wide compensated sum of the lanes' (sum, -comp) pairs, rounded to float
-__device__ __forceinline__ float warp_sum_comp(float sum, float comp) {
-    float hi = sum, lo = -comp;
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-        const float ohi = __shfl_xor_sync(0xffffffffu, hi, off), olo = __shfl_xor_sync(0xffffffffu, lo, off);
-        two_sum_merge(hi, lo, ohi, olo);
-    }
-    return __fadd_rn(hi, lo);
-}
 
 __device__ __forceinline__ int plane_bit(const uint32_t* __restrict__ planes, const AAArgs& A, int b, int c, int y,
                                          int x) {
@@ -211,20 +155,6 @@ __device__ __forceinline__ bool aa_prep(const AAArgs& A, int b, int h, int w, fl
     P.c = c;
     P.c01 = c01;
     return true;
-}
-
-// Gaussian window constants of antialias.cu:121-131
-struct AAWin {
-    float cc, alpha, kr2;
-};
-
-__device__ __forceinline__ AAWin aa_win(float kr) {
-    AAWin q;
-    const float sigma = __fdiv_rn(kr, 4.f);
-    q.cc = __fdiv_rn(1.f, __fmul_rn(__fmul_rn(__fmul_rn(sigma, sigma), 2.f), 3.14159265358979323846f));
-    q.alpha = __fdiv_rn(0.5f, __fmul_rn(sigma, sigma));
-    q.kr2 = __fmul_rn(kr, kr);
-    return q;
 }
 
 // The window of one fragment evaluated by one thread from cluster planes: its rows in
@@ -351,15 +281,9 @@ __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w
     return true;
 }
 
-// Chain rule of one fragment in FP32 (antialias.cu:281-316): (d/dx, d/dy, d/dw) of the
-// edge point; false if not finite
+// Chain rule of one fragment (antialias.cu:281-316)
 __device__ __forceinline__ bool aa_chain(const AAArgs& A, const AAFrag& f, float& dpx, float& dpy, float& dpw) {
-    const float dx = __fmul_rn(__fmul_rn(__fmul_rn(f.dc, 0.5f), (float)A.W), f.nrm.x);
-    const float dy = __fmul_rn(__fmul_rn(__fmul_rn(f.dc, -0.5f), (float)A.H), f.nrm.y);
-    dpx = __fdiv_rn(dx, f.pw);
-    dpy = __fdiv_rn(dy, f.pw);
-    dpw = __fdiv_rn(__fmaf_rn(dx, f.px, __fmul_rn(dy, f.py)), __fmul_rn(f.pw, f.pw));
-    return isfinite(dpx) && isfinite(dpy) && isfinite(dpw);
+    return aa_chain_rule(A.H, A.W, f.dc, f.nrm, f.px, f.py, f.pw, dpx, dpy, dpw);
 }
 
 // antialias.cu:121-279, one warp per fragment of a fragment list

@@ -203,6 +203,18 @@ __device__ __forceinline__ float dda_z(float4 p0, float4 p1, float t1) {
 
 __device__ __forceinline__ bool z_ok(float z) { return isfinite(z) && z >= -1.f && z <= 1.f; }
 
+// Depth test skipped when both ends are finite, 1e-30 <= w <= 1e30 and |z| <= 0.999 w:
+// then for every t1 in [0, 1] the reference's z = (t0 z0 + t1 z1) / (t0 w0 + t1 w1),
+// rounded, has |z| <= 0.999 (1 + 5 eps) < 1, so every fragment passes.
+__device__ __forceinline__ bool depth_always_passes(float4 a, float4 b) {
+    auto ok = [](float4 p) {
+        return isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w >= 1e-30f && p.w <= 1e30f &&
+               fabsf(p.z) <= 0.999f * p.w;
+    };
+    return ok(a) && ok(b);
+}
+
+
 // The reference carries the primitive id as float(e + 1) and casts it back.
 __device__ __forceinline__ int prim_roundtrip(int e) { return f2i((float)(e + 1)) - 1; }
 

@@ -136,17 +136,6 @@ __device__ __forceinline__ int cluster_of(const int32_t* __restrict__ p2c, int e
     return c >= 0 && c < 32 * S ? c : -1;
 }
 
-// Depth test skipped when both ends are finite, 1e-30 <= w <= 1e30 and |z| <= 0.999 w:
-// then for every t1 in [0, 1] the reference's z = (t0 z0 + t1 z1) / (t0 w0 + t1 w1),
-// rounded, has |z| <= 0.999 (1 + 5 eps) < 1, so every fragment passes.
-__device__ __forceinline__ bool depth_always_passes(float4 a, float4 b) {
-    auto ok = [](float4 p) {
-        return isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && p.w >= 1e-30f && p.w <= 1e30f &&
-               fabsf(p.z) <= 0.999f * p.w;
-    };
-    return ok(a) && ok(b);
-}
-
 // A primitive with its cluster entry; craw = p2c[prim_roundtrip(e)], or INT_MIN where that
 // id is outside [0, E).
 struct Lane {
