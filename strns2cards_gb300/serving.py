@@ -12,6 +12,13 @@ jobs' kernels overlap on the GPU.  Requests that arrive while others run wait in
 and are admitted, oldest first, as soon as the HBM budget has room for their footprint;
 a finished job's memory is released before the next admission.
 
+The scheduling thread never waits for the GPU or for host preparation: an admitted job's
+preparation (pinned copies of its inputs, the card edge topology, the target's DDA and
+cluster planes) runs on a worker thread, on the job's stream, and the job joins the
+rounds when it is ready; per-iteration losses stay on the device; a finished job's
+results are copied into pinned host memory asynchronously and collected when its event
+has completed.
+
 ``serve(requests, budget_bytes)`` replays a timed request stream (arrival offsets in
 seconds) and returns per-job latency (completion - arrival) and results;
 ``serve_serial`` runs the same jobs one after another with the plain per-call path.
@@ -89,8 +96,10 @@ class JobResult:
     finished: float = 0.0
     card_pos: Optional[np.ndarray] = None
     loss: List[int] = field(default_factory=list)
-    iou_inter: Optional[np.ndarray] = None
+    iou_inter: Optional[np.ndarray] = None          # per-card counts after the last iteration
     iou_union: Optional[np.ndarray] = None
+    iou_first_inter: Optional[np.ndarray] = None    # ... and of the first iteration
+    iou_first_union: Optional[np.ndarray] = None
 
     @property
     def latency(self) -> float:
@@ -98,12 +107,20 @@ class JobResult:
 
 
 class _Active:
-    """Device state of an admitted job."""
+    """Device state of an admitted job.  ``prepare()`` (any thread) uploads the inputs and
+    builds the target's planes on the job's stream; ``iterate()`` enqueues one iteration;
+    ``start_finish()`` enqueues the copies of the results into pinned host memory and
+    ``collect()`` reads them once ``finished()``."""
 
     def __init__(self, spec: JobSpec, dev, stream):
         self.spec = spec
+        self.dev = dev
         self.stream = stream
         self.done_iters = 0
+        self.ready = None    # Future of prepare() when prepared on a worker thread
+
+    def prepare(self):
+        spec, dev, stream = self.spec, self.dev, self.stream
         H = W = spec.res
         S = (spec.clusters + 31) // 32
         L = _lib.lib()
@@ -115,11 +132,11 @@ class _Active:
             edges, e2t = build_edges_from_triangles(spec.card_tri)
             self.edges, self.e2t = t(edges), t(e2t)
             self.e2c = t(spec.card_t2c[e2t[:, 0]].astype(np.int32))
-            self.target = dda_cluster_bitset((H, W), spos, sedges, se2c, spec.clusters)
+            target = dda_cluster_bitset((H, W), spos, sedges, se2c, spec.clusters)
             del spos, sedges, se2c
             # the target's cluster planes stay resident for the whole job
-            self.tplanes = _core.bitset_to_planes(self.target)
-            del self.target
+            self.tplanes = _core.bitset_to_planes(target)
+            del target
             self.pplanes = torch.empty_like(self.tplanes)
             self.shape = (1, H, W, S)
             self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(1, H, W, self.tri.shape[0]),
@@ -127,8 +144,10 @@ class _Active:
             self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_planes_workspace_size(
                 1, self.cpos.shape[1], self.edges.shape[0]), dtype=torch.uint8, device=dev)
             self.d_pos = torch.zeros_like(self.cpos)
-            self.losses = []
+            self.losses = torch.zeros(max(spec.iterations, 1), dtype=torch.int64, device=dev)
+            self.iou_first = None
             self.iou = None
+        return self
 
     def iterate(self):
         spec = self.spec
@@ -136,67 +155,108 @@ class _Active:
             # the iteration in cluster-plane layout (the target's planes were built at admission)
             _core.rasterize_fused_planes(self.cpos, self.tri, self.t2c, spec.clusters, spec.res, spec.res,
                                          planes=self.pplanes, ws=self.ws_tri)
-            self.losses.append(_core.xor_popcount(self.pplanes, self.tplanes))
+            self.losses[self.done_iters:self.done_iters + 1].copy_(_core.xor_popcount(self.pplanes, self.tplanes))
             self.d_pos.zero_()
             _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, self.shape, self.cpos, self.tri,
                                                          self.edges, self.e2t, self.e2c, 7.0, 0.5, d_pos=self.d_pos,
                                                          ws=self.ws_aa)
             self.iou = _core.cluster_iou_counts_planes(self.pplanes, self.tplanes, self.shape, spec.clusters)
+            if self.done_iters == 0:
+                self.iou_first = self.iou
             step_towards(self.cpos, self.d_pos, spec.lr, spec.res)
         self.done_iters += 1
 
-    def finish(self, res: JobResult):
+    def start_finish(self):
+        """Asynchronous copies of the results into pinned host memory, then an event."""
         with torch.cuda.stream(self.stream):
-            res.card_pos = self.cpos.cpu().numpy()
-            res.loss = [int(x.item()) for x in self.losses]
-            res.iou_inter = self.iou[0].cpu().numpy()
-            res.iou_union = self.iou[1].cpu().numpy()
+            src = {"card_pos": self.cpos, "loss": self.losses[:self.done_iters]}
+            if self.iou is not None:
+                src.update(iou_inter=self.iou[0], iou_union=self.iou[1], iou_first_inter=self.iou_first[0],
+                           iou_first_union=self.iou_first[1])
+            self.host = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in src.items()}
+            for k, v in src.items():
+                self.host[k].copy_(v, non_blocking=True)
+            self.event = torch.cuda.Event()
+            self.event.record(self.stream)
+
+    def finished(self) -> bool:
+        return self.event.query()
+
+    def collect(self, res: "JobResult"):
+        h = self.host
+        res.card_pos = h["card_pos"].numpy()
+        res.loss = [int(x) for x in h["loss"].tolist()]
+        if "iou_inter" in h:
+            res.iou_inter, res.iou_union = h["iou_inter"].numpy(), h["iou_union"].numpy()
+            res.iou_first_inter, res.iou_first_union = h["iou_first_inter"].numpy(), h["iou_first_union"].numpy()
+
+    def finish(self, res: "JobResult"):
+        self.start_finish()
+        self.event.synchronize()
+        self.collect(res)
 
 
 def serve(requests: List[JobSpec], budget_bytes: int, device="cuda", max_active: int = 32,
-          realtime: bool = True) -> List[JobResult]:
+          realtime: bool = True, prep_workers: int = 2) -> List[JobResult]:
     """Continuous batching over a timed request stream; returns results in request order."""
+    from concurrent.futures import ThreadPoolExecutor
     dev = torch.device(device)
     order = sorted(range(len(requests)), key=lambda i: requests[i].arrival)
     results = [JobResult(r.name, r.arrival) for r in requests]
     pending: List[int] = []
+    preparing = {}
     active = {}
+    finishing = {}
     used = 0
     streams = [torch.cuda.Stream(device=dev) for _ in range(max_active)]
     free_streams = list(range(max_active))
     t0 = time.perf_counter()
     nxt = 0
-    while nxt < len(order) or pending or active:
-        now = time.perf_counter() - t0
-        while nxt < len(order) and (requests[order[nxt]].arrival <= now or not realtime):
-            pending.append(order[nxt])
-            nxt += 1
-        # admit, oldest first, while the budget and the stream pool allow
-        while pending and free_streams:
-            i = pending[0]
-            need = requests[i].footprint()
-            if used + need > budget_bytes and active:
-                break
-            pending.pop(0)
-            used += need
-            sid = free_streams.pop()
-            results[i].admitted = time.perf_counter() - t0
-            active[i] = (_Active(requests[i], dev, streams[sid]), sid, need)
-        if not active:
-            if nxt < len(order):
-                time.sleep(max(0.0, min(0.005, requests[order[nxt]].arrival - now)))
-            continue
-        # one iteration of every active job, each on its own stream
-        for i, (job, sid, need) in list(active.items()):
-            job.iterate()
-        for i, (job, sid, need) in list(active.items()):
-            if job.done_iters >= job.spec.iterations:
-                job.finish(results[i])                      # synchronises the job's stream
-                results[i].finished = time.perf_counter() - t0
-                del active[i]
-                used -= need
-                free_streams.append(sid)
-                del job
+    with ThreadPoolExecutor(max_workers=max(prep_workers, 1)) as pool:
+        while nxt < len(order) or pending or preparing or active or finishing:
+            now = time.perf_counter() - t0
+            while nxt < len(order) and (requests[order[nxt]].arrival <= now or not realtime):
+                pending.append(order[nxt])
+                nxt += 1
+            # admit, oldest first, while the budget and the stream pool allow; the job is
+            # prepared on a worker thread and joins the rounds when ready
+            while pending and free_streams:
+                i = pending[0]
+                need = requests[i].footprint()
+                if used + need > budget_bytes and (active or preparing or finishing):
+                    break
+                pending.pop(0)
+                used += need
+                sid = free_streams.pop()
+                results[i].admitted = time.perf_counter() - t0
+                job = _Active(requests[i], dev, streams[sid])
+                job.ready = pool.submit(job.prepare)
+                preparing[i] = (job, sid, need)
+            for i, (job, sid, need) in list(preparing.items()):
+                if job.ready.done():
+                    job.ready.result()          # re-raises a preparation error
+                    active[i] = preparing.pop(i)
+            # one iteration of every active job, each on its own stream
+            for i, (job, sid, need) in list(active.items()):
+                job.iterate()
+                if job.done_iters >= job.spec.iterations:
+                    job.start_finish()
+                    finishing[i] = active.pop(i)
+            # collect the finished jobs whose copies have landed; release their memory
+            for i, (job, sid, need) in list(finishing.items()):
+                if job.finished():
+                    job.collect(results[i])
+                    results[i].finished = time.perf_counter() - t0
+                    del finishing[i]
+                    used -= need
+                    free_streams.append(sid)
+                    del job
+            if not active:
+                # nothing to issue this round: wait a little for arrivals, preparations, copies
+                wait = 0.0005
+                if nxt < len(order) and not (pending or preparing or finishing):
+                    wait = max(0.0, min(0.005, requests[order[nxt]].arrival - (time.perf_counter() - t0)))
+                time.sleep(wait)
     torch.cuda.synchronize()
     return results
 
@@ -213,7 +273,7 @@ def serve_serial(requests: List[JobSpec], device="cuda", realtime: bool = True) 
         if realtime and requests[i].arrival > now:
             time.sleep(requests[i].arrival - now)
         results[i].admitted = time.perf_counter() - t0
-        job = _Active(requests[i], dev, stream)
+        job = _Active(requests[i], dev, stream).prepare()
         for _ in range(requests[i].iterations):
             job.iterate()
         job.finish(results[i])
