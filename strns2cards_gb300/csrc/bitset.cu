@@ -175,73 +175,104 @@ __global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, i
 // ---- cluster planes ----------------------------------------------------------------------
 // planes (B, 32 S, H, WQ) uint32, WQ = ceil(W / 32): bit (x & 31) of word x >> 5 of row y
 // of plane c is bit c of pixel (y, x).  A CTA takes one image row, 512 pixels and 8 slots:
-// the tile is read with whole 32-byte runs per pixel, each warp turns (32 pixels x 32
-// clusters) blocks around with a 5-stage shuffle bit transpose, and the plane rows are
-// written contiguously.
+// the tile is read with whole 32-byte runs per pixel (16-byte loads), each thread turns one
+// (32 pixels x 32 clusters) block around in registers, and the plane rows are written
+// contiguously.
 constexpr int kPlaneX = 512, kPlaneS = 8;
+constexpr int kPlaneG = kPlaneX / 32;                   // pixel groups per tile
+constexpr int kPlaneThreads = kPlaneG * kPlaneS;        // one thread per 32 x 32 block
+constexpr int kTinRow = kPlaneS + 1;                    // input tile: word (p, s) at
+constexpr int kTinGrp = 32 * kTinRow + 8;               //   (p / 32) * kTinGrp + (p % 32) * kTinRow + s
+constexpr int kToutRow = kPlaneG + 1;                   // output tile: word (s, c, g) at
+constexpr int kToutSlot = 32 * kToutRow + 4;            //   s * kToutSlot + c * kToutRow + g
 
-__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
-    // recursive block swap: after the stage for j, blocks j x j apart are exchanged
+// 32 x 32 bit transpose in registers: on return bit i of a[c] is bit c of the input a[i].
+// Five stages swap the off-diagonal J x J blocks of every 2J x 2J block (J = 16 .. 1).
+template <int J, uint32_t M>
+__device__ __forceinline__ void transpose_stage(uint32_t (&a)[32]) {
 #pragma unroll
-    for (int j = 16; j; j >>= 1) {
-        const uint32_t m = j == 16 ? 0xFFFF0000u : j == 8 ? 0xFF00FF00u : j == 4 ? 0xF0F0F0F0u
-                         : j == 2 ? 0xCCCCCCCCu : 0xAAAAAAAAu;
-        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
-        x = (lane & j) ? ((x & m) | ((y >> j) & ~m)) : ((x & ~m) | ((y << j) & m));
+    for (int k = 0; k < 32; k += 2 * J) {
+#pragma unroll
+        for (int i = 0; i < J; ++i) {
+            const uint32_t t = ((a[k + i] >> J) ^ a[k + i + J]) & M;
+            a[k + i + J] ^= t;
+            a[k + i] ^= t << J;
+        }
     }
-    return x;
 }
 
-__global__ void __launch_bounds__(256) bitset_to_planes_kernel(int B, int H, int W, int S,
-                                                               const int32_t* __restrict__ bitset,
-                                                               uint32_t* __restrict__ planes) {
-    __shared__ uint32_t tin[kPlaneX][kPlaneS + 1];
-    __shared__ uint32_t tout[kPlaneS][32][kPlaneX / 32 + 1];
+__device__ __forceinline__ void transpose32_regs(uint32_t (&a)[32]) {
+    transpose_stage<16, 0x0000FFFFu>(a);
+    transpose_stage<8, 0x00FF00FFu>(a);
+    transpose_stage<4, 0x0F0F0F0Fu>(a);
+    transpose_stage<2, 0x33333333u>(a);
+    transpose_stage<1, 0x55555555u>(a);
+}
+
+__global__ void __launch_bounds__(kPlaneThreads) bitset_to_planes_kernel(int B, int H, int W, int S,
+                                                                        const int32_t* __restrict__ bitset,
+                                                                        uint32_t* __restrict__ planes) {
+    __shared__ uint32_t tin[kPlaneG * kTinGrp];
+    __shared__ uint32_t tout[kPlaneS * kToutSlot];
     const int WQ = (W + 31) >> 5;
     const int nxt = (W + kPlaneX - 1) / kPlaneX;
     const int xt = blockIdx.x % nxt, st = blockIdx.x / nxt;
     const int x0 = xt * kPlaneX, s0 = st * kPlaneS;
     const int y = blockIdx.y, b = blockIdx.z;
     const int64_t row = ((int64_t)b * H + y) * W;
+    const int tid = threadIdx.x;
     if ((S & 3) == 0 && (((uintptr_t)bitset) & 15) == 0) {
         // 16-byte loads: pixel p's 8 slots are two int4 (S a multiple of 4)
-        for (int i = threadIdx.x; i < kPlaneX * (kPlaneS / 4); i += blockDim.x) {
+#pragma unroll 4
+        for (int i = tid; i < kPlaneX * (kPlaneS / 4); i += kPlaneThreads) {
             const int p = i >> 1, h = i & 1;
-            const int x = x0 + p, s = s0 + 4 * h;
+            const int x = x0 + p, sl = s0 + 4 * h;
             int4 v = make_int4(0, 0, 0, 0);
-            if (x < W && s < S) v = __ldg((const int4*)(bitset + (row + x) * S + s));
-            tin[p][4 * h] = (uint32_t)v.x;
-            tin[p][4 * h + 1] = (uint32_t)v.y;
-            tin[p][4 * h + 2] = (uint32_t)v.z;
-            tin[p][4 * h + 3] = (uint32_t)v.w;
+            if (x < W && sl < S) v = __ldg((const int4*)(bitset + (row + x) * S + sl));
+            uint32_t* d = tin + (p >> 5) * kTinGrp + (p & 31) * kTinRow + 4 * h;
+            d[0] = (uint32_t)v.x;
+            d[1] = (uint32_t)v.y;
+            d[2] = (uint32_t)v.z;
+            d[3] = (uint32_t)v.w;
         }
     } else {
-        for (int i = threadIdx.x; i < kPlaneX * kPlaneS; i += blockDim.x) {
+        for (int i = tid; i < kPlaneX * kPlaneS; i += kPlaneThreads) {
             const int p = i / kPlaneS, sl = i - p * kPlaneS;
-            const int x = x0 + p, s = s0 + sl;
-            tin[p][sl] = (x < W && s < S) ? (uint32_t)__ldg(bitset + (row + x) * S + s) : 0u;
+            const int x = x0 + p, sg = s0 + sl;
+            tin[(p >> 5) * kTinGrp + (p & 31) * kTinRow + sl] =
+                (x < W && sg < S) ? (uint32_t)__ldg(bitset + (row + x) * S + sg) : 0u;
         }
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;   // warp = slot within the tile
-#pragma unroll 4
-    for (int g = 0; g < kPlaneX / 32; ++g) tout[warp][lane][g] = transpose32(tin[32 * g + lane][warp], lane);
+    {
+        // thread (g, s): pixels 32 g .. 32 g + 31 of slot s (bank of word i: 8 g + s + 9 i,
+        // distinct over a warp's threads for every i)
+        const int g = tid >> 3, sl = tid & 7;
+        uint32_t a[32];
+        const uint32_t* src = tin + g * kTinGrp + sl;
+#pragma unroll
+        for (int i = 0; i < 32; ++i) a[i] = src[i * kTinRow];
+        transpose32_regs(a);
+        uint32_t* dst = tout + sl * kToutSlot + g;
+#pragma unroll
+        for (int c = 0; c < 32; ++c) dst[c * kToutRow] = a[c];
+    }
     __syncthreads();
     const int Kp = 32 * S;
     const int q0 = x0 >> 5;
-    const int nq = min(kPlaneX / 32, WQ - q0);
-    // one plane row segment (16 words) per (slot, bit): 4 threads store 4 words each
-    for (int i = threadIdx.x; i < kPlaneS * 32 * 4; i += blockDim.x) {
+    const int nq = min(kPlaneG, WQ - q0);
+    // one plane row segment (16 words) per (slot, cluster bit): 4 threads store 4 words each
+    for (int i = tid; i < kPlaneS * 32 * 4; i += kPlaneThreads) {
         const int quad = i & 3, bit = (i >> 2) & 31, sl = i >> 7;
-        const int s = s0 + sl;
-        if (s >= S) continue;
-        uint32_t* dst = planes + (((int64_t)b * Kp + 32 * s + bit) * H + y) * WQ + q0;
-        const uint32_t* src = tout[sl][bit];
+        const int sg = s0 + sl;
+        if (sg >= S) continue;
+        uint32_t* dst = planes + (((int64_t)b * Kp + 32 * sg + bit) * H + y) * WQ + q0;
+        const uint32_t* src = tout + sl * kToutSlot + bit * kToutRow;
         const int g0 = 4 * quad;
         if (g0 + 4 <= nq && (((uintptr_t)(dst + g0)) & 15) == 0) {
             *(uint4*)(dst + g0) = make_uint4(src[g0], src[g0 + 1], src[g0 + 2], src[g0 + 3]);
         } else {
-            for (int g = g0; g < g0 + 4 && g < nq; ++g) dst[g] = src[g];
+            for (int gg = g0; gg < g0 + 4 && gg < nq; ++gg) dst[gg] = src[gg];
         }
     }
 }
@@ -370,7 +401,7 @@ extern "C" s2c_status s2c_bitset_to_planes(int B, int H, int W, int S, const int
     const int nxt = (W + kPlaneX - 1) / kPlaneX, nst = (S + kPlaneS - 1) / kPlaneS;
     S2C_REQUIRE((int64_t)nxt * nst < (1LL << 31), "bitset_to_planes: too many tiles");
     dim3 grid((unsigned)(nxt * nst), (unsigned)H, (unsigned)B);
-    bitset_to_planes_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(B, H, W, S, bitset, planes);
+    bitset_to_planes_kernel<<<grid, kPlaneThreads, 0, (cudaStream_t)stream>>>(B, H, W, S, bitset, planes);
     S2C_CHECK_LAUNCH("bitset_to_planes_kernel");
     return S2C_OK;
 }
