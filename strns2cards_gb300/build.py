@@ -23,6 +23,12 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "--fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "-I", INCLUDE, "-I", CSRC]
+# Units whose float outputs are only held to a tolerance (no bit-for-bit cross-check with
+# another unit or with host code) may contract multiply-adds.  Every other unit keeps
+# --fmad=false: coverage, spans, depth and barycentrics must match the reference's FP32
+# arithmetic bit for bit, and frames.cu / curves.cu share device code whose results are
+# compared bit for bit with each other and with the host resampler.
+CONTRACT = {"deform.cu"}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
@@ -49,7 +55,8 @@ def _compile(src: str, force: bool, hdr_mtime: float):
     if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), hdr_mtime):
         return obj, None
     if src.endswith(".cu"):
-        cmd = [_nvcc(), *ARCH, *NVCC_FLAGS, "-c", path, "-o", obj]
+        flags = [f for f in NVCC_FLAGS if not (src in CONTRACT and f == "--fmad=false")]
+        cmd = [_nvcc(), *ARCH, *flags, "-c", path, "-o", obj]
     else:
         cmd = [os.environ.get("CXX", "g++"), *CXX_FLAGS, "-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -274,3 +274,56 @@ def test_raster_into_planes_and_plane_iou():
     i2, u2 = _core.cluster_iou_counts_planes(planes, op, tuple(bits.shape), K)
     assert torch.equal(i1, i2) and torch.equal(u1, u2)
     assert int(_core.xor_popcount(planes, op)) == int(_core.xor_popcount(bits, other))
+
+
+def test_rasterize_fused_rows_on_hard_triangles():
+    """The fused raster tests only the columns of each bounding-box row that the triangle's
+    projection can reach (with a pixel of margin); triangles that are collinear, zero-area,
+    sub-pixel, slivers, far larger than the view, in perspective or with a corner behind
+    the camera must still give the list path's rast and bitset exactly."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    rng = np.random.default_rng(77)
+    B, H, W = 2, 97, 131
+    groups = []
+    n = 120
+    base = rng.uniform(-1.1, 1.1, size=(n, 3, 4))
+    base[..., 3] = 1.0
+    groups.append(base)                                                  # ordinary
+    col = base.copy()
+    t = rng.uniform(0, 1, size=(n, 1))
+    col[:, 2, :2] = col[:, 0, :2] + t * (col[:, 1, :2] - col[:, 0, :2])   # collinear corners
+    groups.append(col)
+    tiny = base.copy()
+    tiny[:, 1:, :2] = tiny[:, :1, :2] + rng.normal(scale=1e-3, size=(n, 2, 2))   # sub-pixel
+    groups.append(tiny)
+    sliver = base.copy()
+    sliver[:, 2, :2] = 0.5 * (sliver[:, 0, :2] + sliver[:, 1, :2]) + rng.normal(scale=2e-4, size=(n, 2))
+    groups.append(sliver)
+    same = base.copy()
+    same[:, 1] = same[:, 0]                                             # two equal corners
+    groups.append(same)
+    huge = base.copy()
+    huge[..., :2] *= 50.0                                               # far beyond the view
+    groups.append(huge)
+    persp = base.copy()
+    persp[..., 3] = rng.uniform(0.05, 2.0, size=(n, 3))
+    persp[..., :2] *= persp[..., 3:4]
+    groups.append(persp)
+    behind = persp.copy()
+    behind[::3, 1, 3] = -0.3                                            # a corner behind the camera
+    groups.append(behind)
+    tris = np.concatenate(groups, 0)                                    # (T, 3, 4)
+    tris[..., 2] = rng.uniform(-0.9, 0.9, size=tris.shape[:2]) * np.abs(tris[..., 3])
+    T = tris.shape[0]
+    pos = np.stack([tris.reshape(-1, 4), (tris * [[[1.0, -1.0, 1.0, 1.0]]]).reshape(-1, 4)]).astype(np.float32)
+    tri = np.arange(3 * T, dtype=np.int32).reshape(T, 3)
+    t2c = (np.arange(T) % 70).astype(np.int32)
+    fp, fa = s2c.compute_fragments((H, W), cu(pos), cu(tri))
+    rast = s2c.depth_test(B, (H, W), fp, fa)
+    ref_bits = torch.zeros((B, H, W, 3), dtype=torch.int32, device="cuda")
+    _core.cluster_mask_from_fragments(fp, fa, cu(t2c), ref_bits)
+    frast, fbits = s2c.rasterize_fused((H, W), cu(pos), cu(tri), cu(t2c), 70)
+    assert torch.equal(fbits, ref_bits)
+    assert torch.equal(frast, rast)
+    assert int((rast[..., 3] > 0).sum()) > 1000
