@@ -850,14 +850,17 @@ def batched_numbers(steps, warmup=3, plain_iters=2, trials=3):
     torch.cuda.synchronize()
     plain_rate = C * plain_iters / (a.elapsed_time(b) / 1e3)
     del plain
-    # end to end: card and strand positions in from pinned host memory, cards out
-    sp = torch.from_numpy(batch.strand_pos).pin_memory()
+    # end to end: card and strand positions in from pinned host memory, cards out (the
+    # strands as the applied schedule reads them: packed for the persistent launch)
+    packed = fit.mode.startswith("persistent")
+    sp = torch.from_numpy(fit.spos_packed_h if packed else batch.strand_pos).pin_memory()
+    sp_dev = fit.spos_packed if packed else fit.spos
     cp = torch.from_numpy(batch.card_pos).pin_memory()
     out = torch.empty(cp.shape, dtype=torch.float32).pin_memory()
     # the schedule stays applied (its graph, or the eager sequence)
 
     def e2e_step():
-        fit.spos.copy_(sp, non_blocking=True)
+        sp_dev.copy_(sp, non_blocking=True)
         fit.cpos.copy_(cp, non_blocking=True)
         fit.step()
         out.copy_(fit.cpos, non_blocking=True)

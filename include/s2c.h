@@ -126,6 +126,8 @@ S2C_API s2c_status s2c_dda_cluster_bitset_noalloc(int64_t num_prims, const int32
  * cluster c owning edge_ids[cluster_offsets[c] .. cluster_offsets[c + 1]); cards card_pos
  * (C, Vc, 4), updated in place, sharing card_tri (Tc, 3), card_edges / card_edge2tri (Ec, 2)
  * and the Laplacian neighbour CSR of one card (lap_offsets (Vc + 1), lap_adj (nadj)).
+ * With vert_offsets (C + 1) non-NULL the strand vertices are packed instead: cluster c's are
+ * strand_pos rows vert_offsets[c] .. vert_offsets[c + 1] (Vs is then unused).
  * Per cluster: the strands' DDA coverage (exact, as dda_compute_fragments +
  * cluster_mask_from_fragments), the card raster's coverage (exact), the antialiased-bitset
  * gradient d_pos (FP64 sums), x, y -= d_pos * (step_scale / max |d_pos.xy|), then
@@ -137,7 +139,8 @@ S2C_API s2c_status s2c_dda_cluster_bitset_noalloc(int64_t num_prims, const int32
  * stream by each call; calls sharing one workspace must not overlap. */
 S2C_API size_t s2c_fit_smem_bytes(int H, int W, int Vc, int Ec, int nadj);
 S2C_API size_t s2c_fit_workspace_size(int C, int H, int W);
-S2C_API s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float* strand_pos, int Es,
+S2C_API s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float* strand_pos,
+                                     const int32_t* vert_offsets, int Es,
                                      const int32_t* strand_edges, const int32_t* edge_ids,
                                      const int32_t* cluster_offsets, int Vc, float* card_pos,
                                      int Tc, const int32_t* card_tri, int Ec,

@@ -39,8 +39,8 @@ SIGNATURES = {
     "s2c_dda_cluster_bitset_noalloc": ([c_i64, vp, c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_i, vp, vp], c_i),
     "s2c_fit_smem_bytes": ([c_i, c_i, c_i, c_i, c_i], c_sz),
     "s2c_fit_workspace_size": ([c_i, c_i, c_i], c_sz),
-    "s2c_fit_iteration": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, c_i, vp,
-                           c_i, c_i, vp, c_f, c_f, c_i, c_f, c_f, c_i, c_i, c_i, vp, c_sz, vp], c_i),
+    "s2c_fit_iteration": ([c_i, c_i, c_i, c_i, vp, vp, c_i, vp, vp, vp, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, c_i,
+                           vp, c_i, c_i, vp, c_f, c_f, c_i, c_f, c_f, c_i, c_i, c_i, vp, c_sz, vp], c_i),
     "s2c_compute_triangle_rects_workspace_size": ([c_i, c_i], c_sz),
     "s2c_compute_triangle_rects": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, vp, c_sz, i64p, vp], c_i),
     "s2c_compute_fragments": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i64, vp, vp, vp], c_i),

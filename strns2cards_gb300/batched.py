@@ -142,6 +142,21 @@ class BatchedClusterFit:
         self.seg_counts = np.bincount(owner, minlength=C).astype(np.int64)[:C]
         self.coff = t(np.concatenate([[0], np.cumsum(self.seg_counts)]).astype(np.int32))
         self.ws_fit = torch.empty(L.s2c_fit_workspace_size(C, H, W), dtype=torch.uint8, device=dev)
+        # the persistent launch reads strand vertices packed: cluster c's used vertices (up to
+        # the largest index its segments reference) at rows voff[c] .. voff[c + 1]
+        used = np.zeros(C, np.int64)
+        if batch.edge_ids.size:
+            mine = owner < C
+            seg_max = batch.strand_edges[batch.edge_ids[mine] % max(E, 1)].max(1).astype(np.int64) + 1
+            np.maximum.at(used, owner[mine], seg_max)
+        used = np.minimum(used, batch.strand_pos.shape[1])
+        self.voff_h = np.concatenate([[0], np.cumsum(used)]).astype(np.int64)
+        if self.voff_h[-1] >= 2 ** 31:
+            raise ValueError("BatchedClusterFit: more than 2^31 - 1 packed strand vertices.")
+        self.voff = t(self.voff_h.astype(np.int32))
+        self.spos_packed_h = np.concatenate([batch.strand_pos[c, :used[c]] for c in range(C)]) if C else \
+            np.zeros((0, 4), np.float32)
+        self.spos_packed = t(self.spos_packed_h)
         self.step_scale = float(np.float32(2.0 * self.lr / max(H, W)))
         self.params = dict(chunk=8192, threads=256, ctas_per_sm=2, aa_warp=0)
         self._items: Dict[int, tuple] = {}
@@ -186,7 +201,7 @@ class BatchedClusterFit:
         p = dict(self.params, **(params or {}))
         items, nch, n_items = self.items(int(p["chunk"]))
         lap = self.lap
-        _lib.call("s2c_fit_iteration", self.C, self.H, self.W, self.spos.shape[1], _lib.ptr(self.spos),
+        _lib.call("s2c_fit_iteration", self.C, self.H, self.W, 0, _lib.ptr(self.spos_packed), _lib.ptr(self.voff),
                   self.sedges.shape[0], _lib.ptr(self.sedges), _lib.ptr(self.edge_ids), _lib.ptr(self.coff),
                   self.cpos.shape[1], _lib.ptr(self.cpos), self.ctri.shape[0], _lib.ptr(self.ctri),
                   self.cedges.shape[0], _lib.ptr(self.cedges), _lib.ptr(self.ce2t), _lib.ptr(lap.offsets),

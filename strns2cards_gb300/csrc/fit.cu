@@ -33,9 +33,11 @@ namespace s2c {
 
 struct FitArgs {
     int C, H, W, WQ;
-    // strands: positions (C, Vs) and one shared polyline edge list; edge_ids[i] = c * Es + e
-    // grouped by cluster, cluster c owning [coff[c], coff[c + 1])
+    // strands: positions (C, Vs) -- or, with voff, cluster c's vertices at
+    // [voff[c], voff[c + 1]) of one packed array -- and one shared polyline edge list;
+    // edge_ids[i] = c * Es + e grouped by cluster, cluster c owning [coff[c], coff[c + 1])
     const float4* __restrict__ spos;
+    const int32_t* __restrict__ voff;
     int Vs, Es;
     const int2* __restrict__ sedges;
     const int32_t* __restrict__ edge_ids;
@@ -128,8 +130,14 @@ __device__ __forceinline__ void fit_cover_segment(const FitArgs& a, int c, int32
     const int pr = prim_roundtrip(e);       // the reference carries the id as float(e + 1)
     if (pr < 0 || pr >= a.Es) return;
     const int2 ev = __ldg(a.sedges + e);
-    if ((unsigned)ev.x >= (unsigned)a.Vs || (unsigned)ev.y >= (unsigned)a.Vs) return;
-    const float4 p0 = __ldg(a.spos + (int64_t)b * a.Vs + ev.x), p1 = __ldg(a.spos + (int64_t)b * a.Vs + ev.y);
+    int64_t v0 = (int64_t)b * a.Vs;
+    int nv = a.Vs;
+    if (a.voff) {
+        v0 = __ldg(a.voff + b);
+        nv = __ldg(a.voff + b + 1) - (int)v0;
+    }
+    if ((unsigned)ev.x >= (unsigned)nv || (unsigned)ev.y >= (unsigned)nv) return;
+    const float4 p0 = __ldg(a.spos + v0 + ev.x), p1 = __ldg(a.spos + v0 + ev.y);
     const Span s = dda_span(p0, p1, a.H, a.W);
     const bool zfast = depth_always_passes(p0, p1);
     for (int k = 0; k < s.count; ++k) {
@@ -509,7 +517,8 @@ extern "C" size_t s2c_fit_workspace_size(int C, int H, int W) {
     return cv.off + 256;
 }
 
-extern "C" s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float* strand_pos, int Es,
+extern "C" s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float* strand_pos,
+                                        const int32_t* vert_offsets, int Es,
                                         const int32_t* strand_edges, const int32_t* edge_ids,
                                         const int32_t* cluster_offsets, int Vc, float* card_pos, int Tc,
                                         const int32_t* card_tri, int Ec, const int32_t* card_edges,
@@ -567,6 +576,7 @@ extern "C" s2c_status s2c_fit_iteration(int C, int H, int W, int Vs, const float
     a.W = W;
     a.WQ = WQ;
     a.spos = (const float4*)strand_pos;
+    a.voff = vert_offsets;
     a.Vs = Vs;
     a.Es = Es;
     a.sedges = (const int2*)strand_edges;

@@ -5,7 +5,8 @@ iteration equals the eager launch sequence.  The persistent launch (one kernel p
 iteration) gives the same iterations as the launch sequence, for every launch shape the
 autotuner may choose (chunks of the largest clusters split over CTAs, one thread or one
 warp per antialias fragment, 128 to 1024 threads), with empty clusters and frames whose
-width is not a multiple of 32; the tuner's choice is cached per shape class."""
+width is not a multiple of 32, reading the strands packed (each cluster's used vertices only);
+the tuner's choice is cached per shape class."""
 import os
 
 import numpy as np
@@ -90,6 +91,8 @@ def test_persistent_empty_cluster_and_ragged_width():
     batch.edge_ids = batch.edge_ids[batch.edge_ids // E != 2]          # cluster 2 has no strands
     fa, fb = _persistent_vs_eager(batch, dict(chunk=300, threads=256, ctas_per_sm=2, aa_warp=1))
     assert close(fb.cpos, fa.cpos)
+    # the persistent launch reads the strands packed: no rows for the empty cluster
+    assert fb.voff_h[3] == fb.voff_h[2] and fb.spos_packed.shape[0] < batch.strand_pos.shape[0] * batch.strand_pos.shape[1]
 
 
 def test_persistent_graph_replay_and_tuning_cache(tmp_path):
