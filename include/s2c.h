@@ -335,8 +335,8 @@ S2C_API s2c_status s2c_backward_antialiased_cluster_bitset_f64(
  * fragment list and no host synchronisation (capturable in a CUDA graph).  Same
  * contributions as mark_discontinuity_edges + dda_compute_fragments + the backward above;
  * d_pos (B, V, 4) accumulated.  The workspace holds the FP64 accumulator (B*V*3 doubles)
- * and the cluster planes of both bitsets (see s2c_bitset_to_planes), read by the windows.
- * At most 2^32 - 1 silhouette fragments per call. */
+ * and the cluster planes of both bitsets (see s2c_bitset_to_planes), read by the windows;
+ * it must be 16-byte aligned.  At most 2^32 - 1 silhouette fragments per call. */
 S2C_API size_t s2c_antialiased_cluster_bitset_grad_workspace_size(int B, int V, int H, int W, int S, int E);
 S2C_API s2c_status s2c_antialiased_cluster_bitset_grad(
     int B, int H, int W, int S, const int32_t* bitset, const int32_t* target, int V, const float* pos, int T,
@@ -344,7 +344,8 @@ S2C_API s2c_status s2c_antialiased_cluster_bitset_grad(
     float* d_pos, float kernel_radius, float rho, void* workspace, size_t workspace_bytes, s2c_stream stream);
 
 /* new: the same from cluster planes the caller keeps (e.g. the target's, built once per fit);
- * workspace: the FP64 accumulator (B*V*3 doubles) and per-(view, edge) work counts. */
+ * workspace (16-byte aligned): the FP64 accumulator (B*V*3 doubles), per-(view, edge) work
+ * counts and an 80-byte record per silhouette (view, edge) (end points, span, normal). */
 S2C_API size_t s2c_antialiased_cluster_bitset_grad_planes_workspace_size(int B, int V, int E);
 S2C_API s2c_status s2c_antialiased_cluster_bitset_grad_planes(
     int B, int H, int W, int S, const uint32_t* bitset_planes, const uint32_t* target_planes, int V,

@@ -157,38 +157,6 @@ __device__ __forceinline__ bool aa_prep(const AAArgs& A, int b, int h, int w, fl
     return true;
 }
 
-// The window of one fragment evaluated by one thread from cluster planes: its rows in
-// order, each as the 1-2 plane words covering [w0, w1) of both images, visiting only the
-// pixels where they differ; Kahan FP32 sum.  Returns dc (0 when nothing contributes).
-__device__ __forceinline__ float aa_window_thread(const AAArgs& A, int b, const AAPrep& P, const AAWin& q) {
-    float sum = 0.f, comp = 0.f;
-    if (P.w1 <= P.w0) return 0.f;
-    const int64_t pbase = ((int64_t)b * 32 * A.S + P.c) * A.H;
-    const int q0 = P.w0 >> 5, q1 = (P.w1 - 1) >> 5;
-    for (int th = P.h0; th < P.h1; ++th) {
-        const uint32_t* prow = A.pplanes + (pbase + th) * A.WQ;
-        const uint32_t* trow = A.tplanes + (pbase + th) * A.WQ;
-        const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), P.fy);
-        for (int qq = q0; qq <= q1; ++qq) {
-            const int lo = max(P.w0 - 32 * qq, 0), hi = min(P.w1 - 32 * qq, 32);
-            const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
-            const uint32_t pv = __ldg(prow + qq), tv = __ldg(trow + qq);
-            const uint32_t pos = pv & ~tv & m;
-            uint32_t any = (pv ^ tv) & m;
-            while (any) {
-                const int bit = __ffs(any) - 1;
-                any &= any - 1;
-                const float dx = __fsub_rn(__fadd_rn((float)(32 * qq + bit), 0.5f), P.fx);
-                const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
-                if (!(n2 < q.kr2)) continue;
-                const float wgt = __fmul_rn(q.cc, expf(-q.alpha * n2));
-                kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, A.rho) : -wgt);
-            }
-        }
-    }
-    return __fmul_rn((float)P.c01, __fsub_rn(sum, comp));
-}
-
 template <bool kPlanes>
 __device__ __forceinline__ bool aa_fragment(const AAArgs& A, int b, int h, int w, float axis, float t1, int e,
                                             float2 nrm, int lane, AAFrag& o) {
@@ -328,16 +296,44 @@ __global__ void __launch_bounds__(256) aa_backward_kernel(AAArgs A) {
 }
 
 // Fused edge gradient.  Pass 1 (thread per (view, edge)): the mark test and the DDA span
-// count (the fragments dda_compute_fragments would list for the edge); a device scan;
-// pass 2: one thread per fragment.  Warps take equal chunks of the global fragment index
-// space; each lane of a warp holds one edge of a sliding window of 32 (its prefix, mark
-// normal, span and end points, computed once per edge) and every fragment takes its
-// owner's data by shuffles, regenerates its pixel with the DDA arithmetic (coverage is
-// recomputed, not stored), evaluates its window from the cluster planes and adds its
-// FP32 chain-rule contributions to the FP64 accumulator.
+// count (the fragments dda_compute_fragments would list for the edge); a silhouette edge
+// also leaves a record (end points, span, normal) for pass 2.  A device scan.  Pass 2
+// (aa_frag_kernel): warps take equal chunks of the global fragment index space, 32
+// fragments at a time:
+//  1. each lane regenerates one fragment from its owner edge's record (the owner found by
+//     a shuffle search over a 32-edge window of prefixes) with the DDA arithmetic --
+//     coverage is recomputed, not stored -- and sets up its window (aa_prep);
+//  2. the warp shares the window rows of its (up to 32) fragments: row i of the flattened
+//     list goes to lane i % 32, which reads the 1-2 plane words of both images, visits the
+//     pixels where they differ and leaves the row's compensated sum in shared memory.  A
+//     thread per window would leave lanes idle while the warp's heaviest window finishes
+//     (window work varies from nothing to the whole disk), and lanes whose fragment
+//     contributes nothing would idle throughout;
+//  3. each fragment's lane merges its rows' sums in row order (deterministic), applies the
+//     chain rule and adds the contributions to the FP64 accumulator.
 constexpr int kAAFragChunk = 64;
+constexpr int kAARowCap = 256;    // row sums held per warp between merges
 
-__global__ void __launch_bounds__(256) aa_count_kernel(AAArgs A, Mesh M, int32_t* __restrict__ counts) {
+// a silhouette edge as pass 2 reads it
+struct alignas(16) AAEdgeRec {
+    float4 p0, p1;
+    float sx, sy, slope, off0;
+    float off1, axis;
+    int count, b;
+    float nx, ny;
+    int e, pad;
+};
+
+// a fragment's window as the row-sharing lanes read it
+struct AARowDesc {
+    float fx, fy;
+    int h0, first;      // first: the fragment's first row in the warp's flattened list
+    int w0, w1;
+    int64_t rowbase;    // word offset of row 0 of the fragment's cluster plane
+};
+
+__global__ void __launch_bounds__(256) aa_count_kernel(AAArgs A, Mesh M, int32_t* __restrict__ counts,
+                                                       AAEdgeRec* __restrict__ recs) {
     const int64_t BE = (int64_t)A.B * M.E;
     for (int64_t pe = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pe < BE; pe += (int64_t)gridDim.x * blockDim.x) {
         const int b = (int)M.divE.div((uint32_t)pe);
@@ -346,47 +342,67 @@ __global__ void __launch_bounds__(256) aa_count_kernel(AAArgs A, Mesh M, int32_t
         int n = 0;
         if (mark_edge(A.H, A.W, M, b, e, nrm) == 2) {
             const int2 ev = __ldg(M.edges + e);
-            n = dda_span(__ldg(M.pos4 + (int64_t)b * M.V + ev.x), __ldg(M.pos4 + (int64_t)b * M.V + ev.y), A.H,
-                         A.W).count;
+            const float4 p0 = __ldg(M.pos4 + (int64_t)b * M.V + ev.x), p1 = __ldg(M.pos4 + (int64_t)b * M.V + ev.y);
+            const Span sp = dda_span(p0, p1, A.H, A.W);
+            n = sp.count;
+            if (n > 0) {
+                AAEdgeRec r;
+                r.p0 = p0;
+                r.p1 = p1;
+                r.sx = sp.sx;
+                r.sy = sp.sy;
+                r.slope = sp.slope;
+                r.off0 = sp.off0;
+                r.off1 = sp.off1;
+                r.axis = sp.axis;
+                r.count = sp.count;
+                r.b = b;
+                r.nx = nrm.x;
+                r.ny = nrm.y;
+                r.e = e;
+                r.pad = 0;
+                recs[pe] = r;
+            }
         }
         counts[pe] = n;
     }
 }
 
-// one lane's edge of the window
-struct AAEdge {
-    float4 p0, p1;
-    Span sp;
-    float2 nrm;
-    int b, e;
-};
-
-__device__ __forceinline__ void aa_load_edge(const AAArgs& A, const Mesh& M, int64_t pe, int64_t BE, AAEdge& g) {
-    g.b = 0;
-    g.e = -1;
-    g.sp.count = 0;
-    if (pe >= BE) return;
-    g.b = (int)M.divE.div((uint32_t)pe);
-    g.e = (int)pe - g.b * M.E;
-    if (mark_edge(A.H, A.W, M, g.b, g.e, g.nrm) != 2) {
-        g.e = -1;
-        return;
+// One window row of a fragment: the pixels of [w0, w1) where the two planes differ, each
+// weighted by the Gaussian (antialias.cu:177-206), as a Kahan FP32 sum (sum - comp).
+__device__ __forceinline__ float2 aa_window_row(const AAArgs& A, const AARowDesc& r, int th, const AAWin& q) {
+    const uint32_t* prow = A.pplanes + r.rowbase + (int64_t)th * A.WQ;
+    const uint32_t* trow = A.tplanes + r.rowbase + (int64_t)th * A.WQ;
+    const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), r.fy);
+    float sum = 0.f, comp = 0.f;
+    for (int qq = r.w0 >> 5; qq <= (r.w1 - 1) >> 5; ++qq) {
+        const int lo = max(r.w0 - 32 * qq, 0), hi = min(r.w1 - 32 * qq, 32);
+        const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
+        const uint32_t pv = __ldg(prow + qq), tv = __ldg(trow + qq);
+        const uint32_t pos = pv & ~tv & m;
+        uint32_t any = (pv ^ tv) & m;
+        while (any) {
+            const int bit = __ffs(any) - 1;
+            any &= any - 1;
+            const float dx = __fsub_rn(__fadd_rn((float)(32 * qq + bit), 0.5f), r.fx);
+            const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+            if (!(n2 < q.kr2)) continue;
+            const float wgt = __fmul_rn(q.cc, expf(-q.alpha * n2));
+            kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, A.rho) : -wgt);
+        }
     }
-    const int2 ev = __ldg(M.edges + g.e);
-    g.p0 = __ldg(M.pos4 + (int64_t)g.b * M.V + ev.x);
-    g.p1 = __ldg(M.pos4 + (int64_t)g.b * M.V + ev.y);
-    g.sp = dda_span(g.p0, g.p1, A.H, A.W);
+    return make_float2(sum, -comp);
 }
 
-__device__ __forceinline__ float4 shfl4(float4 v, int src) {
-    return make_float4(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
-                       __shfl_sync(0xffffffffu, v.z, src), __shfl_sync(0xffffffffu, v.w, src));
-}
-
-__global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, Mesh M, const uint32_t* __restrict__ prefix,
+__global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, const AAEdgeRec* __restrict__ recs,
+                                                      const uint32_t* __restrict__ prefix,
                                                       const int64_t* __restrict__ total) {
+    __shared__ AARowDesc s_desc[256];
+    __shared__ float2 s_rows[8 * kAARowCap];
     const int lane = threadIdx.x & 31;
-    const int64_t BE = (int64_t)A.B * M.E;
+    AARowDesc* dsc = s_desc + (threadIdx.x & ~31);
+    float2* rows_sum = s_rows + (threadIdx.x >> 5) * kAARowCap;
+    const int64_t BE = (int64_t)A.B * A.E;
     const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int64_t tot64 = *total;
@@ -406,8 +422,6 @@ __global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, Mesh M, const
         int64_t t0 = lo;
         uint32_t start = t0 > 0 ? __ldg(prefix + t0 - 1) : 0u;
         uint32_t pre = t0 + lane < BE ? __ldg(prefix + t0 + lane) : 0xffffffffu;
-        AAEdge g;
-        aa_load_edge(A, M, t0 + lane, BE, g);
         uint32_t base = c0;
         while (base < c1) {
             for (;;) {
@@ -417,7 +431,6 @@ __global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, Mesh M, const
                 start = __shfl_sync(0xffffffffu, pre, adv - 1);
                 t0 += adv;
                 pre = t0 + lane < BE ? __ldg(prefix + t0 + lane) : 0xffffffffu;
-                aa_load_edge(A, M, t0 + lane, BE, g);
             }
             const uint32_t wend = __shfl_sync(0xffffffffu, pre, 31);
             const uint32_t end = min(min(c1, base + 32u), wend);
@@ -429,52 +442,96 @@ __global__ void __launch_bounds__(256, 4) aa_frag_kernel(AAArgs A, Mesh M, const
                 if (pv <= j) ow += step;
             }
             const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
-            // the owner edge's data, from its lane
-            const float4 p0 = shfl4(g.p0, ow), p1 = shfl4(g.p1, ow);
-            Span sp;
-            sp.sx = __shfl_sync(0xffffffffu, g.sp.sx, ow);
-            sp.sy = __shfl_sync(0xffffffffu, g.sp.sy, ow);
-            sp.slope = __shfl_sync(0xffffffffu, g.sp.slope, ow);
-            sp.off0 = __shfl_sync(0xffffffffu, g.sp.off0, ow);
-            sp.off1 = __shfl_sync(0xffffffffu, g.sp.off1, ow);
-            sp.axis = __shfl_sync(0xffffffffu, g.sp.axis, ow);
-            sp.count = __shfl_sync(0xffffffffu, g.sp.count, ow);
-            const float2 nrm = make_float2(__shfl_sync(0xffffffffu, g.nrm.x, ow), __shfl_sync(0xffffffffu, g.nrm.y, ow));
-            const int b = __shfl_sync(0xffffffffu, g.b, ow), e = __shfl_sync(0xffffffffu, g.e, ow);
             base = end;
-            if (j >= end || e < 0) continue;
-            const int k = (int)(j - (ow > 0 ? prev : start));
-            if (k >= sp.count) continue;
-            float x, y;
-            dda_sample(sp, k, x, y);
-            const int h = f2i(floorf(y)), w = f2i(floorf(x));
-            if (h < 0 || h >= A.H || w < 0 || w >= A.W) continue;
-            const float t1 = dda_t1(p0, p1, x, y, sp.axis, A.H, A.W);
-            if (!z_ok(dda_z(p0, p1, t1))) continue;
-            const int ee = prim_roundtrip(e);
+            // 1. this lane's fragment: the owner edge's record (the owner, j < end, has a
+            //    non-zero count and so a record from pass 1 of this call)
             AAPrep P;
-            if (!aa_prep<true>(A, b, h, w, sp.axis, t1, ee, nrm, P)) continue;
-            AAFrag f;
-            f.dc = aa_window_thread(A, b, P, win);
-            if (f.dc == 0.f) continue;
-            f.px = P.px;
-            f.py = P.py;
-            f.pw = P.pw;
-            f.t0 = P.t0;
-            f.t1 = P.t1;
-            f.nrm = P.nrm;
-            f.ev = P.ev;
+            bool ok = false;
+            int b = 0;
+            if (j < end) {
+                const AAEdgeRec g = recs[t0 + ow];
+                b = g.b;
+                Span sp;
+                sp.sx = g.sx;
+                sp.sy = g.sy;
+                sp.slope = g.slope;
+                sp.off0 = g.off0;
+                sp.off1 = g.off1;
+                sp.axis = g.axis;
+                sp.count = g.count;
+                const int k = (int)(j - (ow > 0 ? prev : start));
+                if (g.e >= 0 && k < sp.count) {
+                    float x, y;
+                    dda_sample(sp, k, x, y);
+                    const int h = f2i(floorf(y)), w = f2i(floorf(x));
+                    if (h >= 0 && h < A.H && w >= 0 && w < A.W) {
+                        const float t1 = dda_t1(g.p0, g.p1, x, y, sp.axis, A.H, A.W);
+                        if (z_ok(dda_z(g.p0, g.p1, t1)))
+                            ok = aa_prep<true>(A, b, h, w, sp.axis, t1, prim_roundtrip(g.e), make_float2(g.nx, g.ny),
+                                               P);
+                    }
+                }
+            }
+            // 2. the warp's window rows, flattened: fragment f owns rows [first_f, last_f)
+            const int nrows = ok && P.w1 > P.w0 ? P.h1 - P.h0 : 0;
+            int last = nrows;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, last, d);
+                if (lane >= d) last += v;
+            }
+            const int all = __shfl_sync(0xffffffffu, last, 31);
+            const int first = last - nrows;
+            if (nrows) {
+                AARowDesc r;
+                r.fx = P.fx;
+                r.fy = P.fy;
+                r.h0 = P.h0;
+                r.first = first;
+                r.w0 = P.w0;
+                r.w1 = P.w1;
+                r.rowbase = ((int64_t)b * 32 * A.S + P.c) * A.H * A.WQ;
+                dsc[lane] = r;
+            }
+            __syncwarp();
+            float shi = 0.f, slo = 0.f;
+            for (int r0 = 0; r0 < all; r0 += kAARowCap) {
+                const int r1 = min(all, r0 + kAARowCap);
+                for (int i0 = r0; i0 < r1; i0 += 32) {
+                    const int i = i0 + lane;
+                    int o = 0;   // the fragment of row i: the first lane whose last > i
+#pragma unroll
+                    for (int step = 16; step; step >>= 1) {
+                        const int v = __shfl_sync(0xffffffffu, last, o + step - 1);
+                        if (v <= i) o += step;
+                    }
+                    if (i >= r1) continue;
+                    const AARowDesc r = dsc[o];
+                    rows_sum[i - r0] = aa_window_row(A, r, r.h0 + (i - r.first), win);
+                }
+                __syncwarp();
+                // 3. this fragment's rows of the batch, in order
+                for (int i = max(first, r0); i < min(last, r1); ++i) {
+                    const float2 v = rows_sum[i - r0];
+                    two_sum_merge(shi, slo, v.x, v.y);
+                }
+                __syncwarp();
+            }
+            if (!nrows) continue;
+            const float dc = __fmul_rn((float)P.c01, __fadd_rn(shi, slo));
+            if (dc == 0.f) continue;
             float dpx, dpy, dpw;
-            if (!aa_chain(A, f, dpx, dpy, dpw)) continue;
-            double* a0 = A.acc64 + ((int64_t)b * A.V + f.ev.x) * 3;
-            double* a1 = A.acc64 + ((int64_t)b * A.V + f.ev.y) * 3;
-            atomicAdd(a0 + 0, (double)__fmul_rn(dpx, f.t0));
-            atomicAdd(a0 + 1, (double)__fmul_rn(dpy, f.t0));
-            atomicAdd(a0 + 2, (double)__fmul_rn(dpw, f.t0));
-            atomicAdd(a1 + 0, (double)__fmul_rn(dpx, f.t1));
-            atomicAdd(a1 + 1, (double)__fmul_rn(dpy, f.t1));
-            atomicAdd(a1 + 2, (double)__fmul_rn(dpw, f.t1));
+            if (!aa_chain_rule(A.H, A.W, dc, P.nrm, P.px, P.py, P.pw, dpx, dpy, dpw)) continue;
+            double* a0 = A.acc64 + ((int64_t)b * A.V + P.ev.x) * 3;
+            double* a1 = A.acc64 + ((int64_t)b * A.V + P.ev.y) * 3;
+            atomicAdd(a0 + 0, (double)__fmul_rn(dpx, P.t0));
+            atomicAdd(a0 + 1, (double)__fmul_rn(dpy, P.t0));
+            atomicAdd(a0 + 2, (double)__fmul_rn(dpw, P.t0));
+            atomicAdd(a1 + 0, (double)__fmul_rn(dpx, P.t1));
+            atomicAdd(a1 + 1, (double)__fmul_rn(dpy, P.t1));
+            atomicAdd(a1 + 2, (double)__fmul_rn(dpw, P.t1));
         }
+        __syncwarp();
     }
 }
 
@@ -603,6 +660,7 @@ struct AAWs {
     int32_t* prefix;
     int64_t* total;
     void* scan;
+    AAEdgeRec* recs;
 };
 
 size_t aa_carve(int B, int V, int E, void* base, size_t cap, AAWs* w) {
@@ -614,6 +672,7 @@ size_t aa_carve(int B, int V, int E, void* base, size_t cap, AAWs* w) {
     a.prefix = cv.take<int32_t>(BE);
     a.total = cv.take<int64_t>(1);
     a.scan = cv.take<char>(scan_workspace_bytes(BE));
+    a.recs = cv.take<AAEdgeRec>(BE);
     if (w) *w = a;
     return cv.off;
 }
@@ -636,7 +695,7 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
                     (T == 0 || tri) && workspace,
                 "antialiased_cluster_bitset_grad: null pointer");
     S2C_REQUIRE(((uintptr_t)pos & 15) == 0 && ((uintptr_t)edges & 7) == 0 && ((uintptr_t)edge2tri & 7) == 0 &&
-                    ((uintptr_t)workspace & 7) == 0,
+                    ((uintptr_t)workspace & 15) == 0,
                 "antialiased_cluster_bitset_grad: misaligned");
     S2C_REQUIRE(kernel_radius >= 0.f && kernel_radius < 1024.f, "antialiased_cluster_bitset_grad: bad kernel_radius");
     AAWs ws;
@@ -673,11 +732,11 @@ extern "C" s2c_status s2c_antialiased_cluster_bitset_grad_planes(
     A.WQ = (W + 31) / 32;
     A.kr = kernel_radius;
     A.rho = rho;
-    aa_count_kernel<<<grid_for(BE, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(A, M, ws.chunks);
+    aa_count_kernel<<<grid_for(BE, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(A, M, ws.chunks, ws.recs);
     S2C_CHECK_LAUNCH("aa_count_kernel");
     s2c_status ss = inclusive_scan_i32(ws.chunks, BE, ws.prefix, ws.scan, ws.total, st);
     if (ss != S2C_OK) return ss;
-    aa_frag_kernel<<<num_sms() * 8, 256, 0, st>>>(A, M, (const uint32_t*)ws.prefix, ws.total);
+    aa_frag_kernel<<<num_sms() * 8, 256, 0, st>>>(A, ws.recs, (const uint32_t*)ws.prefix, ws.total);
     S2C_CHECK_LAUNCH("aa_frag_kernel");
     aa_finalize_kernel<<<grid_for(BV, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(BV, ws.acc, d_pos);
     S2C_CHECK_LAUNCH("aa_finalize_kernel");
