@@ -55,8 +55,11 @@ def test_mark_discontinuity_edges_bit_exact():
     assert np.array_equal(np_(cids), ref[ref >= 0])
 
 
-@pytest.mark.parametrize("tag,kr,rho", [("r7", 7.0, 0.5), ("r3", 3.5, 1.0)])
+@pytest.mark.parametrize("tag,kr,rho", [("r7", 7.0, 0.5), ("r3", 3.5, 1.0), ("r15", 15.9, 0.5), ("r17", 17.0, 0.8)])
 def test_antialias_gradient(tag, kr, rho):
+    """Fused gradient == list path == FP64 oracle (and the reference's recorded gradient where
+    the fixture has one), for radii whose windows span 7 to 35 pixels per row (one to three
+    plane words per row)."""
     import strns2cards_gb300 as s2c
     a = golden("antialias.npz")
     args = [cu(a[k]) for k in ("bitset", "target", "pos", "tri", "edges", "edge2tri", "edge2cluster")]
@@ -76,8 +79,9 @@ def test_antialias_gradient(tag, kr, rho):
     ok, err = grad_close(got, ora)
     assert ok, err
     assert np.array_equal(got != 0, ora != 0)
-    ok, err = grad_close(got, a["d_pos_" + tag], tol=2e-5)
-    assert ok, err
+    if "d_pos_" + tag in a:
+        ok, err = grad_close(got, a["d_pos_" + tag], tol=2e-5)
+        assert ok, err
 
 
 def test_antialias_float_atomic_entry():
@@ -161,7 +165,7 @@ def test_cluster_iou_counts_large_and_ragged(shape, K):
     assert np.array_equal(np_(inter), ri) and np.array_equal(np_(uni), ru)
 
 
-@pytest.mark.parametrize("shape", [(2, 5, 700, 3), (1, 33, 64, 64), (1, 3, 31, 1)])
+@pytest.mark.parametrize("shape", [(2, 5, 700, 3), (1, 33, 64, 64), (1, 3, 31, 1), (1, 4, 300, 20), (2, 2, 513, 36)])
 def test_bitset_to_planes(shape):
     """Cluster planes: bit (x & 31) of word x >> 5 in row y of plane c = bit c of pixel (y, x);
     ragged widths, several x tiles, odd slot counts."""
