@@ -76,6 +76,24 @@ __device__ __forceinline__ float warp_sum_comp(float sum, float comp) {
     return __fadd_rn(hi, lo);
 }
 
+// Border rows / columns of a window whose offset alone reaches the disk's edge hold no
+// pixel with n2 = fma(dx, dx, dy * dy) < kr^2 (n2 >= fl(dy * dy) and n2 >= fl(dx * dx), with
+// d = (t + 0.5) - f as the window sums compute it): dropping them changes no sum.  With the
+// half-pixel test, one axis's offsets are whole numbers and its two border lines sit exactly
+// on the edge.
+__device__ __forceinline__ float aa_off2(int t, float f) {
+    const float d = __fsub_rn(__fadd_rn((float)t, 0.5f), f);
+    return __fmul_rn(d, d);
+}
+
+__device__ __forceinline__ void aa_trim_window(float kr, float fx, float fy, int& h0, int& h1, int& w0, int& w1) {
+    const float kr2 = __fmul_rn(kr, kr);
+    while (h0 < h1 && !(aa_off2(h0, fy) < kr2)) ++h0;
+    while (h1 > h0 && !(aa_off2(h1 - 1, fy) < kr2)) --h1;
+    while (w0 < w1 && !(aa_off2(w0, fx) < kr2)) ++w0;
+    while (w1 > w0 && !(aa_off2(w1 - 1, fx) < kr2)) --w1;
+}
+
 // Gaussian window constants of antialias.cu:121-131
 struct AAWin {
     float cc, alpha, kr2;

@@ -143,19 +143,7 @@ __device__ __forceinline__ bool aa_prep(const AAArgs& A, int b, int h, int w, fl
     P.h1 = min(ch + R, A.H - 1) + 1;
     P.w0 = max(cw - R, 0);
     P.w1 = min(cw + R, A.W - 1) + 1;
-    // Border rows / columns whose offset alone reaches the disk's edge hold no pixel with
-    // n2 = fma(dx, dx, dy * dy) < kr^2 (n2 >= fl(dy * dy) and n2 >= fl(dx * dx)): dropping
-    // them changes no sum.  With the half-pixel test, one axis's offsets are whole numbers
-    // and its two border lines sit exactly on the edge.
-    const float kr2 = __fmul_rn(A.kr, A.kr);
-    auto off2 = [](int t, float f) {
-        const float d = __fsub_rn(__fadd_rn((float)t, 0.5f), f);
-        return __fmul_rn(d, d);
-    };
-    while (P.h0 < P.h1 && !(off2(P.h0, fy) < kr2)) ++P.h0;
-    while (P.h1 > P.h0 && !(off2(P.h1 - 1, fy) < kr2)) --P.h1;
-    while (P.w0 < P.w1 && !(off2(P.w0, fx) < kr2)) ++P.w0;
-    while (P.w1 > P.w0 && !(off2(P.w1 - 1, fx) < kr2)) --P.w1;
+    aa_trim_window(A.kr, fx, fy, P.h0, P.h1, P.w0, P.w1);
     P.fx = fx;
     P.fy = fy;
     P.px = px;

@@ -198,6 +198,7 @@ __device__ __forceinline__ bool fit_frag_prep(const FitArgs& a, const FitSmem& S
     P.h1 = min(ch + R, a.H - 1) + 1;
     P.w0 = max(cw - R, 0);
     P.w1 = min(cw + R, a.W - 1) + 1;
+    aa_trim_window(a.kr, fx, fy, P.h0, P.h1, P.w0, P.w1);
     P.fx = fx;
     P.fy = fy;
     P.px = px;
