@@ -177,16 +177,16 @@ __global__ void __launch_bounds__(256) cluster_iou_kernel(int64_t npix, int S, i
 // of plane c is bit c of pixel (y, x).  A CTA takes one image row, 256 pixels and 16 slots:
 // the tile is read with whole 64-byte runs per pixel (16-byte loads), each thread turns one
 // (32 pixels x 32 clusters) block around in registers, and the plane rows are written
-// contiguously.  The input and output tiles share one shared-memory buffer (18.5 KB), so
-// about 11 CTAs fit an SM and keep enough loads in flight: 0.109 ms per 256 MiB on GB300
+// contiguously.  The input and output tiles share one shared-memory buffer (16.5 KB), so
+// about 12 CTAs fit an SM and keep enough loads in flight: 0.109 ms per 256 MiB on GB300
 // (4.9 TB/s); 512 x 8 tiles took 0.117 ms shared and 0.171 ms with separate buffers.
 constexpr int kPlaneX = 256, kPlaneS = 16;
 constexpr int kPlaneG = kPlaneX / 32;                   // pixel groups per tile
 constexpr int kPlaneThreads = kPlaneG * kPlaneS;        // one thread per 32 x 32 block
-constexpr int kTinRow = kPlaneS + 1;                    // input tile: word (p, s) at
-constexpr int kTinGrp = 32 * kTinRow + kPlaneS;         //   (p / 32) * kTinGrp + (p % 32) * kTinRow + s
-constexpr int kToutRow = kPlaneG + 1;                   // output tile: word (s, c, g) at
-constexpr int kToutSlot = 32 * kToutRow + 32 / kPlaneS; //   s * kToutSlot + c * kToutRow + g
+constexpr int kTinRow = kPlaneS;                        // input tile: word (p, s) at
+constexpr int kTinGrp = 32 * kTinRow + 4;               //   (p / 32) * kTinGrp + (p % 32) * kTinRow + s
+constexpr int kToutRow = kPlaneG;                       // output tile: word (s, c, g) at
+constexpr int kToutSlot = 32 * kToutRow + 8;            //   s * kToutSlot + c * kToutRow + g
 constexpr int kPlaneIn = kPlaneG * kTinGrp, kPlaneOut = kPlaneS * kToutSlot;
 constexpr int kPlaneV4 = kPlaneS / 4;                   // 16-byte loads per pixel
 constexpr int kPlaneQ = kPlaneG / 4;                    // 16-byte stores per plane-row segment
@@ -217,7 +217,7 @@ __device__ __forceinline__ void transpose32_regs(uint32_t (&a)[32]) {
 __global__ void __launch_bounds__(kPlaneThreads) bitset_to_planes_kernel(int B, int H, int W, int S,
                                                                         const int32_t* __restrict__ bitset,
                                                                         uint32_t* __restrict__ planes) {
-    __shared__ uint32_t tbuf[kPlaneIn > kPlaneOut ? kPlaneIn : kPlaneOut];
+    __shared__ __align__(16) uint32_t tbuf[kPlaneIn > kPlaneOut ? kPlaneIn : kPlaneOut];
     uint32_t* tin = tbuf;     // read into registers, then overwritten by the output tile
     uint32_t* tout = tbuf;
     const int WQ = (W + 31) >> 5;
@@ -235,11 +235,8 @@ __global__ void __launch_bounds__(kPlaneThreads) bitset_to_planes_kernel(int B, 
             const int x = x0 + p, sl = s0 + 4 * h;
             int4 v = make_int4(0, 0, 0, 0);
             if (x < W && sl < S) v = __ldg((const int4*)(bitset + (row + x) * S + sl));
-            uint32_t* d = tin + (p >> 5) * kTinGrp + (p & 31) * kTinRow + 4 * h;
-            d[0] = (uint32_t)v.x;
-            d[1] = (uint32_t)v.y;
-            d[2] = (uint32_t)v.z;
-            d[3] = (uint32_t)v.w;
+            // 16-byte stores: a quarter warp writes two pixels' 16 words, all banks once
+            *(int4*)(tin + (p >> 5) * kTinGrp + (p & 31) * kTinRow + 4 * h) = v;
         }
     } else {
         for (int i = tid; i < kPlaneX * kPlaneS; i += kPlaneThreads) {
@@ -251,10 +248,10 @@ __global__ void __launch_bounds__(kPlaneThreads) bitset_to_planes_kernel(int B, 
     }
     __syncthreads();
     {
-        // thread (g, s): pixels 32 g .. 32 g + 31 of slot s (bank of word i: 16 g + s + 17 i,
-        // distinct over a warp's threads for every i; output bank of cluster c:
-        // 2 s + g + 9 c, distinct as well)
-        const int g = tid / kPlaneS, sl = tid % kPlaneS;
+        // thread (g, s): pixels 32 g .. 32 g + 31 of slot s; a warp holds g = 0..7 of four
+        // slots (bank of input word i: 4 g + s + 16 i, of output word c: 8 s + g + 8 c,
+        // distinct over the warp's threads for every i and c)
+        const int g = tid % kPlaneG, sl = tid / kPlaneG;
         uint32_t a[32];
         const uint32_t* src = tin + g * kTinGrp + sl;
 #pragma unroll
@@ -278,7 +275,7 @@ __global__ void __launch_bounds__(kPlaneThreads) bitset_to_planes_kernel(int B, 
         const uint32_t* src = tout + sl * kToutSlot + bit * kToutRow;
         const int g0 = 4 * quad;
         if (g0 + 4 <= nq && (((uintptr_t)(dst + g0)) & 15) == 0) {
-            *(uint4*)(dst + g0) = make_uint4(src[g0], src[g0 + 1], src[g0 + 2], src[g0 + 3]);
+            *(uint4*)(dst + g0) = *(const uint4*)(src + g0);   // 16-byte aligned: kToutSlot, kToutRow, g0 % 4 == 0
         } else {
             for (int gg = g0; gg < g0 + 4 && gg < nq; ++gg) dst[gg] = src[gg];
         }
