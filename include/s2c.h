@@ -200,6 +200,18 @@ S2C_API s2c_status s2c_rasterize_fused_planes(int B, int H, int W, int V, const 
                                               const int32_t* tri, const int32_t* tri2cluster,
                                               int num_tri2cluster, int S, uint32_t* planes, float* rast,
                                               void* workspace, size_t workspace_bytes, s2c_stream stream);
+/* new: the same pass ORing the cards' cluster bits onto planes the caller keeps (not cleared
+ * here; they must hold zeros wherever this pass can set a bit, e.g. after
+ * s2c_planes_clear_rects with the previous pass's rectangles), and writing cluster_rects
+ * (B, 32 S, 4) int32, 16-byte aligned: per (view, plane) rows [y0, y1) x plane words
+ * [q0, q1) holding every bit it can set (the union of the cluster's triangle rectangles;
+ * empty = (H, 0, ceil(W / 32), 0)).  A fitting loop then clears and counts only those
+ * rectangles instead of whole planes. */
+S2C_API s2c_status s2c_rasterize_fused_planes_onto(int B, int H, int W, int V, const float* pos, int T,
+                                                   const int32_t* tri, const int32_t* tri2cluster,
+                                                   int num_tri2cluster, int S, uint32_t* planes,
+                                                   int32_t* cluster_rects, void* workspace,
+                                                   size_t workspace_bytes, s2c_stream stream);
 S2C_API s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream);
@@ -298,6 +310,23 @@ S2C_API s2c_status s2c_cluster_iou_counts(int64_t num_pixels, int S, int K, cons
 S2C_API s2c_status s2c_cluster_iou_counts_planes(int B, int H, int W, int S, int K, const uint32_t* a,
                                                  const uint32_t* b, uint64_t* inter, uint64_t* uni,
                                                  s2c_stream stream);
+
+/* new: plane rectangles (B, 32 S, 4) int32 (y0, y1, q0, q1), 16-byte aligned: rows
+ * [y0, y1) x plane words [q0, q1) of each (view, plane), clamped to the plane; y0 >= y1 or
+ * q0 >= q1 is empty.  clear_rects zeroes each plane's rectangle; bounds writes the smallest
+ * rectangle holding every non-zero word of each plane (empty = (H, 0, ceil(W / 32), 0)). */
+S2C_API s2c_status s2c_planes_clear_rects(int B, int H, int W, int S, uint32_t* planes, const int32_t* rects,
+                                          s2c_stream stream);
+S2C_API s2c_status s2c_planes_bounds(int B, int H, int W, int S, const uint32_t* planes, int32_t* rects,
+                                     s2c_stream stream);
+/* new: s2c_cluster_iou_counts_planes counting only inside the bounding rectangle of each
+ * plane's rects_a and rects_b rectangles -- exact when every set bit of a (b) lies inside its
+ * rects_a (rects_b) rectangle -- and *xor_total (nullable, device uint64) = the XOR-popcount
+ * loss over all 32 S planes (sum of union - inter), in the same pass. */
+S2C_API s2c_status s2c_cluster_iou_counts_planes_rects(int B, int H, int W, int S, int K, const uint32_t* a,
+                                                       const uint32_t* b, const int32_t* rects_a,
+                                                       const int32_t* rects_b, uint64_t* inter, uint64_t* uni,
+                                                       uint64_t* xor_total, s2c_stream stream);
 
 /* ---------------------------------------------------------------------------------- *
  * antialiased cluster bitset loss                                                     *

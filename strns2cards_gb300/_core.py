@@ -478,6 +478,74 @@ def cluster_iou_counts_planes(a_planes, b_planes, shape, K) -> tuple:
     return inter, uni
 
 
+def rasterize_fused_planes_onto(pos, tri, tri2cluster, cluster_count, H, W, planes, rects=None, ws=None):
+    """The fused card raster ORed onto ``planes`` (not cleared: zeros wherever it can set a
+    bit, e.g. after ``planes_clear_rects`` with the previous pass's rectangles); returns the
+    per-(view, plane) word rectangles (B, 32 S, 4) int32 of every bit it can set."""
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(tri2cluster, _i32, 1, name="tri2cluster")
+    _cuda(pos, tri, tri2cluster, planes)
+    B, V = pos.shape[0], pos.shape[1]
+    S = (int(cluster_count) + 31) // 32
+    shape = (B, 32 * S, H, (W + 31) // 32)
+    if tuple(planes.shape) != shape or not planes.is_contiguous() or planes.dtype != _i32:
+        raise RuntimeError("rasterize_fused_planes_onto: planes must be contiguous int32 " + str(shape))
+    if rects is None:
+        rects = torch.empty((B, 32 * S, 4), dtype=torch.int32, device=pos.device)
+    elif tuple(rects.shape) != (B, 32 * S, 4) or rects.dtype != _i32 or not rects.is_contiguous():
+        raise RuntimeError(f"rasterize_fused_planes_onto: rects must be contiguous int32 {(B, 32 * S, 4)}")
+    need = _lib.lib().s2c_rasterize_fused_workspace_size(B, H, W, tri.shape[0])
+    if ws is None or ws.numel() < need:
+        ws = workspace(need, pos.device)
+    call("s2c_rasterize_fused_planes_onto", B, H, W, V, ptr(pos), tri.shape[0], ptr(tri), ptr(tri2cluster),
+         tri2cluster.shape[0], S, ptr(planes), ptr(rects), ptr(ws), ws.numel(), _stream(pos))
+    return rects
+
+
+def _plane_rects_arg(planes, rects, shape, name):
+    B, H, W, S = shape
+    want = (B, 32 * S, H, (W + 31) // 32)
+    if tuple(planes.shape) != want or not planes.is_contiguous():
+        raise RuntimeError(f"{name}: planes must be contiguous {want}")
+    if rects is not None and (tuple(rects.shape) != (B, 32 * S, 4) or rects.dtype != _i32 or
+                              not rects.is_contiguous()):
+        raise RuntimeError(f"{name}: rects must be contiguous int32 {(B, 32 * S, 4)}")
+
+
+def planes_clear_rects(planes, rects, shape) -> None:
+    """Zero each (view, plane)'s word rectangle (y0, y1, q0, q1); ``shape`` = (B, H, W, S)."""
+    _cuda(planes, rects)
+    _plane_rects_arg(planes, rects, shape, "planes_clear_rects")
+    B, H, W, S = shape
+    call("s2c_planes_clear_rects", B, H, W, S, ptr(planes), ptr(rects), _stream(planes))
+
+
+def planes_bounds(planes, shape, rects=None) -> torch.Tensor:
+    """The smallest word rectangle (y0, y1, q0, q1) holding every non-zero word of each
+    (view, plane); (B, 32 S, 4) int32."""
+    _cuda(planes)
+    B, H, W, S = shape
+    if rects is None:
+        rects = torch.empty((B, 32 * S, 4), dtype=torch.int32, device=planes.device)
+    _plane_rects_arg(planes, rects, shape, "planes_bounds")
+    call("s2c_planes_bounds", B, H, W, S, ptr(planes), ptr(rects), _stream(planes))
+    return rects
+
+
+def cluster_iou_counts_planes_rects(a_planes, b_planes, a_rects, b_rects, shape, K) -> tuple:
+    """Per-cluster (inter, union) counts and the XOR-popcount total, counting only inside each
+    plane's rectangles (exact when every set bit lies inside its plane's rectangle)."""
+    _cuda(a_planes, b_planes, a_rects, b_rects)
+    for pl, r in ((a_planes, a_rects), (b_planes, b_rects)):
+        _plane_rects_arg(pl, r, shape, "cluster_iou_counts_planes_rects")
+    B, H, W, S = shape
+    out = torch.empty(2 * K + 1, dtype=torch.int64, device=a_planes.device)
+    call("s2c_cluster_iou_counts_planes_rects", B, H, W, S, int(K), ptr(a_planes), ptr(b_planes), ptr(a_rects),
+         ptr(b_rects), ptr(out), ptr(out[K:]), ptr(out[2 * K:]), _stream(a_planes))
+    return out[:K], out[K:2 * K], out[2 * K]
+
+
 def bitset_to_planes(bitset, planes=None) -> torch.Tensor:
     """Cluster planes (B, 32 S, H, ceil(W / 32)) int32 of a bitset (B, H, W, S)."""
     _arr(bitset, _i32, 4, name="bitset")

@@ -50,6 +50,10 @@ SIGNATURES = {
     "s2c_rasterize_fused": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_i, c_i, vp, vp, vp, c_sz, vp], c_i),
     "s2c_rasterize_fused_planes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_i, c_i, vp, vp, vp, c_sz, vp], c_i),
     "s2c_cluster_iou_counts_planes": ([c_i, c_i, c_i, c_i, c_i, vp, vp, vp, vp, vp], c_i),
+    "s2c_rasterize_fused_planes_onto": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_i, c_i, vp, vp, vp, c_sz, vp], c_i),
+    "s2c_planes_clear_rects": ([c_i, c_i, c_i, c_i, vp, vp, vp], c_i),
+    "s2c_planes_bounds": ([c_i, c_i, c_i, c_i, vp, vp, vp], c_i),
+    "s2c_cluster_iou_counts_planes_rects": ([c_i, c_i, c_i, c_i, c_i, vp, vp, vp, vp, vp, vp, vp, vp], c_i),
     "s2c_msaa_resolve": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp, vp, vp, vp], c_i),
     "s2c_barycentric_derivatives": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, vp], c_i),
     "s2c_interpolate_triangle_attributes": ([c_i, c_i, c_i, c_i, vp, c_i, vp, c_i, vp, vp, vp], c_i),

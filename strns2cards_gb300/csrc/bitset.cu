@@ -331,6 +331,135 @@ __global__ void __launch_bounds__(256) planes_iou_kernel(int K, int Kp, int64_t 
     }
 }
 
+// ---- plane rectangles ----------------------------------------------------------------
+// A rectangle (y0, y1, q0, q1) per (view, plane): rows [y0, y1) x plane words [q0, q1),
+// clamped to the plane; y0 >= y1 or q0 >= q1 is empty.
+struct PlaneRect {
+    int y0, y1, q0, q1;
+    __device__ __forceinline__ bool empty() const { return y0 >= y1 || q0 >= q1; }
+};
+
+__device__ __forceinline__ PlaneRect plane_rect(const int4* __restrict__ rects, int64_t i, int H, int WQ) {
+    const int4 r = __ldg(rects + i);
+    PlaneRect p;
+    p.y0 = max(r.x, 0);
+    p.y1 = min(r.y, H);
+    p.q0 = max(r.z, 0);
+    p.q1 = min(r.w, WQ);
+    return p;
+}
+
+// the words of a rectangle, one per thread in turn: row-major over (y0..y1) x (q0..q1)
+template <class F>
+__device__ __forceinline__ void for_rect_words(const PlaneRect& r, F f) {
+    if (r.empty()) return;
+    const int nq = r.q1 - r.q0;
+    const int64_t n = (int64_t)(r.y1 - r.y0) * nq;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const int y = r.y0 + (int)(i / nq), q = r.q0 + (int)(i % nq);
+        f(y, q);
+    }
+}
+
+// zero each (view, plane)'s rectangle; one CTA per plane
+__global__ void __launch_bounds__(256) planes_clear_rects_kernel(int Kp, int H, int WQ, uint32_t* __restrict__ planes,
+                                                                 const int4* __restrict__ rects) {
+    const int64_t pl = (int64_t)blockIdx.y * Kp + blockIdx.x;
+    const PlaneRect r = plane_rect(rects, pl, H, WQ);
+    uint32_t* p = planes + pl * H * WQ;
+    for_rect_words(r, [&](int y, int q) { p[(int64_t)y * WQ + q] = 0u; });
+}
+
+// the smallest rectangle holding every non-zero word of each plane; one CTA per plane
+__global__ void __launch_bounds__(256) planes_bounds_kernel(int Kp, int H, int WQ, const uint32_t* __restrict__ planes,
+                                                            int4* __restrict__ rects) {
+    const int64_t pl = (int64_t)blockIdx.y * Kp + blockIdx.x;
+    __shared__ int b[4];
+    if (threadIdx.x == 0) {
+        b[0] = H;
+        b[1] = 0;
+        b[2] = WQ;
+        b[3] = 0;
+    }
+    __syncthreads();
+    const uint32_t* p = planes + pl * H * WQ;
+    const int64_t n = (int64_t)H * WQ;
+    int y0 = H, y1 = 0, q0 = WQ, q1 = 0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        if (__ldcs(p + i) == 0u) continue;
+        const int y = (int)(i / WQ), q = (int)(i % WQ);
+        y0 = min(y0, y);
+        y1 = max(y1, y + 1);
+        q0 = min(q0, q);
+        q1 = max(q1, q + 1);
+    }
+    if (y1 > 0) {
+        atomicMin(b + 0, y0);
+        atomicMax(b + 1, y1);
+        atomicMin(b + 2, q0);
+        atomicMax(b + 3, q1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) rects[pl] = make_int4(b[0], b[1], b[2], b[3]);
+}
+
+// Per-cluster counts over the bounding rectangle of both planes' rectangles (every set bit
+// of either plane lies inside its rectangle); *xor_total += sum over all planes of
+// popc(a ^ b) = union - inter.
+__global__ void __launch_bounds__(256) planes_iou_rects_kernel(int K, int Kp, int H, int WQ,
+                                                               const uint32_t* __restrict__ a,
+                                                               const uint32_t* __restrict__ b,
+                                                               const int4* __restrict__ ra,
+                                                               const int4* __restrict__ rb,
+                                                               unsigned long long* __restrict__ inter,
+                                                               unsigned long long* __restrict__ uni,
+                                                               unsigned long long* __restrict__ xor_total) {
+    const int c = blockIdx.x;
+    const int64_t pl = (int64_t)blockIdx.y * Kp + c;
+    const PlaneRect x = plane_rect(ra, pl, H, WQ), y = plane_rect(rb, pl, H, WQ);
+    PlaneRect r;
+    if (x.empty()) r = y;
+    else if (y.empty()) r = x;
+    else {
+        r.y0 = min(x.y0, y.y0);
+        r.y1 = max(x.y1, y.y1);
+        r.q0 = min(x.q0, y.q0);
+        r.q1 = max(x.q1, y.q1);
+    }
+    const uint32_t* pa = a + pl * H * WQ;
+    const uint32_t* pb = b + pl * H * WQ;
+    unsigned int ni = 0, nu = 0;
+    for_rect_words(r, [&](int yy, int q) {
+        const int64_t i = (int64_t)yy * WQ + q;
+        const uint32_t u = pa[i], v = pb[i];
+        ni += __popc(u & v);
+        nu += __popc(u | v);
+    });
+    for (int o = 16; o; o >>= 1) {
+        ni += __shfl_xor_sync(0xffffffffu, ni, o);
+        nu += __shfl_xor_sync(0xffffffffu, nu, o);
+    }
+    __shared__ unsigned int si[8], su[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        si[warp] = ni;
+        su[warp] = nu;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long ti = 0, tu = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            ti += si[w];
+            tu += su[w];
+        }
+        if (c < K) {
+            if (ti) atomicAdd(inter + c, ti);
+            if (tu) atomicAdd(uni + c, tu);
+        }
+        if (xor_total && tu > ti) atomicAdd(xor_total, tu - ti);
+    }
+}
+
 }  // namespace s2c
 
 using namespace s2c;
@@ -428,5 +557,56 @@ extern "C" s2c_status s2c_cluster_iou_counts_planes(int B, int H, int W, int S, 
                                                                         (unsigned long long*)inter,
                                                                         (unsigned long long*)uni);
     S2C_CHECK_LAUNCH("planes_iou_kernel");
+    return S2C_OK;
+}
+
+static s2c_status check_rects(const char* what, int B, int H, int W, int S, const void* planes, const void* rects) {
+    S2C_REQUIRE(B >= 0 && H >= 0 && W >= 0 && S > 0 && B <= 65535 && 32LL * S <= 2147483647LL, "%s: bad sizes", what);
+    S2C_REQUIRE(planes && rects, "%s: null pointer", what);
+    S2C_REQUIRE(((uintptr_t)rects & 15) == 0, "%s: rects must be 16-byte aligned", what);
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_planes_clear_rects(int B, int H, int W, int S, uint32_t* planes, const int32_t* rects,
+                                             s2c_stream stream) {
+    if (B == 0 || H == 0 || W == 0) return S2C_OK;
+    s2c_status st = check_rects("planes_clear_rects", B, H, W, S, planes, rects);
+    if (st != S2C_OK) return st;
+    planes_clear_rects_kernel<<<dim3((unsigned)(32 * S), (unsigned)B), 256, 0, (cudaStream_t)stream>>>(
+        32 * S, H, (W + 31) / 32, planes, (const int4*)rects);
+    S2C_CHECK_LAUNCH("planes_clear_rects_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_planes_bounds(int B, int H, int W, int S, const uint32_t* planes, int32_t* rects,
+                                        s2c_stream stream) {
+    if (B == 0 || H == 0 || W == 0) return S2C_OK;
+    s2c_status st = check_rects("planes_bounds", B, H, W, S, planes, rects);
+    if (st != S2C_OK) return st;
+    planes_bounds_kernel<<<dim3((unsigned)(32 * S), (unsigned)B), 256, 0, (cudaStream_t)stream>>>(
+        32 * S, H, (W + 31) / 32, planes, (int4*)rects);
+    S2C_CHECK_LAUNCH("planes_bounds_kernel");
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_cluster_iou_counts_planes_rects(int B, int H, int W, int S, int K, const uint32_t* a,
+                                                          const uint32_t* b, const int32_t* rects_a,
+                                                          const int32_t* rects_b, uint64_t* inter, uint64_t* uni,
+                                                          uint64_t* xor_total, s2c_stream stream) {
+    S2C_REQUIRE(K >= 0 && K <= 32 * S, "cluster_iou_counts_planes_rects: bad K");
+    S2C_REQUIRE(inter && uni, "cluster_iou_counts_planes_rects: null output");
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(inter, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(uni, 0, sizeof(uint64_t) * (size_t)K, st);
+    if (e == cudaSuccess && xor_total) e = cudaMemsetAsync(xor_total, 0, sizeof(uint64_t), st);
+    if (e != cudaSuccess) return cuda_status(e, "cluster_iou_counts_planes_rects: memset");
+    if (B == 0 || H == 0 || W == 0) return S2C_OK;
+    s2c_status s1 = check_rects("cluster_iou_counts_planes_rects", B, H, W, S, a, rects_a);
+    if (s1 == S2C_OK) s1 = check_rects("cluster_iou_counts_planes_rects", B, H, W, S, b, rects_b);
+    if (s1 != S2C_OK) return s1;
+    planes_iou_rects_kernel<<<dim3((unsigned)(32 * S), (unsigned)B), 256, 0, st>>>(
+        K, 32 * S, H, (W + 31) / 32, a, b, (const int4*)rects_a, (const int4*)rects_b, (unsigned long long*)inter,
+        (unsigned long long*)uni, (unsigned long long*)xor_total);
+    S2C_CHECK_LAUNCH("planes_iou_rects_kernel");
     return S2C_OK;
 }

@@ -297,8 +297,22 @@ __global__ void __launch_bounds__(256, 4) tri_fused_kernel(FusedRaster F) {
 }
 
 // screen rectangle and area of every (view, triangle)
+// Per (view, cluster plane) word rectangles (y0, y1, q0, q1): rows [y0, y1) and plane
+// words [q0, q1) holding every bit the raster can set (the union of the cluster's triangle
+// rectangles); empty = (H, 0, WQ, 0).
+struct ClusterRects {
+    int4* __restrict__ r;                  // nullable: (B, Kp)
+    const int32_t* __restrict__ t2c;
+    int num_t2c, Kp;
+};
+
+__global__ void cluster_rects_init_kernel(int64_t n, int H, int WQ, int4* __restrict__ r) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        r[i] = make_int4(H, 0, WQ, 0);
+}
+
 __global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B, Tris R, int4* __restrict__ rects,
-                                                            int32_t* __restrict__ areas) {
+                                                            int32_t* __restrict__ areas, ClusterRects CR) {
     const int64_t n = (int64_t)B * R.T;
     for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
          idx += (int64_t)gridDim.x * blockDim.x) {
@@ -308,6 +322,16 @@ __global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B,
         rects[idx] = rc;
         // work units of the balanced raster: pairs of horizontally adjacent pixels per row
         areas[idx] = (int32_t)((uint32_t)rc.y * (((uint32_t)rc.w + 1u) >> 1));
+        if (CR.r && rc.y > 0 && rc.w > 0 && t < CR.num_t2c) {
+            const int c = __ldg(CR.t2c + t);   // the raster's cluster bit for t (raster_covered)
+            if (c >= 0 && c < CR.Kp) {
+                int* q = (int*)(CR.r + (int64_t)b * CR.Kp + c);
+                atomicMin(q + 0, rc.x);
+                atomicMax(q + 1, rc.x + rc.y);
+                atomicMin(q + 2, rc.z >> 5);
+                atomicMax(q + 3, ((rc.z + rc.w - 1) >> 5) + 1);
+            }
+        }
     }
 }
 
@@ -752,13 +776,13 @@ extern "C" size_t s2c_rasterize_fused_workspace_size(int B, int H, int W, int T)
 static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        uint32_t* planes, float* rast, void* workspace, size_t workspace_bytes,
-                                       s2c_stream stream);
+                                       s2c_stream stream, bool clear_planes, int32_t* cluster_rects);
 
 extern "C" s2c_status s2c_rasterize_fused(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                           const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                           float* rast, void* workspace, size_t workspace_bytes, s2c_stream stream) {
     return rasterize_fused_impl(B, H, W, V, pos, T, tri, tri2cluster, num_tri2cluster, S, bitset, nullptr, rast,
-                                workspace, workspace_bytes, stream);
+                                workspace, workspace_bytes, stream, true, nullptr);
 }
 
 extern "C" s2c_status s2c_rasterize_fused_planes(int B, int H, int W, int V, const float* pos, int T,
@@ -766,13 +790,24 @@ extern "C" s2c_status s2c_rasterize_fused_planes(int B, int H, int W, int V, con
                                                  int S, uint32_t* planes, float* rast, void* workspace,
                                                  size_t workspace_bytes, s2c_stream stream) {
     return rasterize_fused_impl(B, H, W, V, pos, T, tri, tri2cluster, num_tri2cluster, S, nullptr, planes, rast,
-                                workspace, workspace_bytes, stream);
+                                workspace, workspace_bytes, stream, true, nullptr);
+}
+
+extern "C" s2c_status s2c_rasterize_fused_planes_onto(int B, int H, int W, int V, const float* pos, int T,
+                                                      const int32_t* tri, const int32_t* tri2cluster,
+                                                      int num_tri2cluster, int S, uint32_t* planes,
+                                                      int32_t* cluster_rects, void* workspace,
+                                                      size_t workspace_bytes, s2c_stream stream) {
+    S2C_REQUIRE(planes && cluster_rects, "rasterize_fused_planes_onto: null planes / cluster_rects");
+    S2C_REQUIRE(((uintptr_t)cluster_rects & 15) == 0, "rasterize_fused_planes_onto: misaligned cluster_rects");
+    return rasterize_fused_impl(B, H, W, V, pos, T, tri, tri2cluster, num_tri2cluster, S, nullptr, planes, nullptr,
+                                workspace, workspace_bytes, stream, false, cluster_rects);
 }
 
 static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* pos, int T, const int32_t* tri,
                                        const int32_t* tri2cluster, int num_tri2cluster, int S, int32_t* bitset,
                                        uint32_t* planes, float* rast, void* workspace, size_t workspace_bytes,
-                                       s2c_stream stream) {
+                                       s2c_stream stream, bool clear_planes, int32_t* cluster_rects) {
     S2C_REQUIRE(B > 0 && H > 0 && W > 0 && H <= 32768 && W <= 32768 && V >= 0 && T >= 0,
                 "rasterize_fused: bad sizes");
     S2C_REQUIRE((int64_t)B * T < (1LL << 31), "rasterize_fused: B*T too large");
@@ -795,9 +830,19 @@ static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* 
         if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset bitset");
     }
     const int WQ = (W + 31) / 32;
-    if (planes) {
+    if (planes && clear_planes) {
         cudaError_t e = cudaMemsetAsync(planes, 0, (size_t)B * 32 * S * H * WQ * 4, st);
         if (e != cudaSuccess) return cuda_status(e, "rasterize_fused: memset planes");
+    }
+    ClusterRects CR;
+    CR.r = (int4*)cluster_rects;
+    CR.t2c = tri2cluster;
+    CR.num_t2c = num_tri2cluster;
+    CR.Kp = 32 * S;
+    if (cluster_rects) {
+        const int64_t n = (int64_t)B * 32 * S;
+        cluster_rects_init_kernel<<<grid_for(n, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(n, H, WQ, CR.r);
+        S2C_CHECK_LAUNCH("cluster_rects_init_kernel");
     }
     Tris R;
     R.pos4 = (const float4*)pos;
@@ -808,7 +853,7 @@ static s2c_status rasterize_fused_impl(int B, int H, int W, int V, const float* 
     const int64_t BT = (int64_t)B * T;
     if (BT > 0 && (rast || bitset || planes)) {
         tri_rect_area_kernel<<<grid_for(BT, 256, (int64_t)num_sms() * 16), 256, 0, st>>>(H, W, B, R, ws.rects,
-                                                                                           ws.areas);
+                                                                                           ws.areas, CR);
         S2C_CHECK_LAUNCH("tri_rect_area_kernel");
         s2c_status s = inclusive_scan_i32(ws.areas, BT, ws.prefix, ws.scan, ws.total, st);
         if (s != S2C_OK) return s;

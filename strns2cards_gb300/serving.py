@@ -134,11 +134,15 @@ class _Active:
             self.e2c = t(spec.card_t2c[e2t[:, 0]].astype(np.int32))
             target = dda_cluster_bitset((H, W), spos, sedges, se2c, spec.clusters)
             del spos, sedges, se2c
-            # the target's cluster planes stay resident for the whole job
+            # the target's cluster planes stay resident for the whole job, with the rectangle
+            # of each plane's set bits; the prediction's planes start empty and each
+            # iteration clears only the rectangles the previous one could have written
+            self.shape = (1, H, W, S)
             self.tplanes = _core.bitset_to_planes(target)
             del target
-            self.pplanes = torch.empty_like(self.tplanes)
-            self.shape = (1, H, W, S)
+            self.trects = _core.planes_bounds(self.tplanes, self.shape)
+            self.pplanes = torch.zeros_like(self.tplanes)
+            self.prects = torch.tensor([H, 0, (W + 31) // 32, 0], dtype=torch.int32, device=dev).repeat(1, 32 * S, 1)
             self.ws_tri = torch.empty(L.s2c_rasterize_fused_workspace_size(1, H, W, self.tri.shape[0]),
                                       dtype=torch.uint8, device=dev)
             self.ws_aa = torch.empty(L.s2c_antialiased_cluster_bitset_grad_planes_workspace_size(
@@ -152,15 +156,20 @@ class _Active:
     def iterate(self):
         spec = self.spec
         with torch.cuda.stream(self.stream):
-            # the iteration in cluster-plane layout (the target's planes were built at admission)
-            _core.rasterize_fused_planes(self.cpos, self.tri, self.t2c, spec.clusters, spec.res, spec.res,
-                                         planes=self.pplanes, ws=self.ws_tri)
-            self.losses[self.done_iters:self.done_iters + 1].copy_(_core.xor_popcount(self.pplanes, self.tplanes))
+            # the iteration in cluster-plane layout (the target's planes were built at admission):
+            # clear the last prediction's rectangles, raster onto the planes (new rectangles),
+            # per-card counts and the XOR loss in one pass over the rectangles, the gradient
+            _core.planes_clear_rects(self.pplanes, self.prects, self.shape)
+            _core.rasterize_fused_planes_onto(self.cpos, self.tri, self.t2c, spec.clusters, spec.res, spec.res,
+                                              self.pplanes, rects=self.prects, ws=self.ws_tri)
+            inter, uni, xor = _core.cluster_iou_counts_planes_rects(self.pplanes, self.tplanes, self.prects,
+                                                                    self.trects, self.shape, spec.clusters)
+            self.losses[self.done_iters:self.done_iters + 1].copy_(xor)
             self.d_pos.zero_()
             _core.antialiased_cluster_bitset_grad_planes(self.pplanes, self.tplanes, self.shape, self.cpos, self.tri,
                                                          self.edges, self.e2t, self.e2c, 7.0, 0.5, d_pos=self.d_pos,
                                                          ws=self.ws_aa)
-            self.iou = _core.cluster_iou_counts_planes(self.pplanes, self.tplanes, self.shape, spec.clusters)
+            self.iou = (inter, uni)
             if self.done_iters == 0:
                 self.iou_first = self.iou
             step_towards(self.cpos, self.d_pos, spec.lr, spec.res)
