@@ -376,7 +376,32 @@ __device__ __forceinline__ float2 aa_window_row(const AAArgs& A, const AARowDesc
     const uint32_t* trow = A.tplanes + r.rowbase + (int64_t)th * A.WQ;
     const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), r.fy);
     float sum = 0.f, comp = 0.f;
-    for (int qq = r.w0 >> 5; qq <= (r.w1 - 1) >> 5; ++qq) {
+    const int q0 = r.w0 >> 5, width = r.w1 - r.w0;
+    if (width <= 32) {
+        // the row as one 32-bit mask from w0 (one or two plane words), so that a lane's
+        // pixels are one flat loop rather than a loop per word
+        const int sh = r.w0 & 31;
+        uint64_t pv = __ldg(prow + q0), tv = __ldg(trow + q0);
+        if (sh + width > 32) {
+            pv |= (uint64_t)__ldg(prow + q0 + 1) << 32;
+            tv |= (uint64_t)__ldg(trow + q0 + 1) << 32;
+        }
+        const uint32_t m = width == 32 ? 0xffffffffu : (1u << width) - 1u;
+        const uint32_t pw = (uint32_t)(pv >> sh) & m, tw = (uint32_t)(tv >> sh) & m;
+        const uint32_t pos = pw & ~tw;
+        uint32_t any = pw ^ tw;
+        while (any) {
+            const int bit = __ffs(any) - 1;
+            any &= any - 1;
+            const float dx = __fsub_rn(__fadd_rn((float)(r.w0 + bit), 0.5f), r.fx);
+            const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+            if (!(n2 < q.kr2)) continue;
+            const float wgt = __fmul_rn(q.cc, expf(-q.alpha * n2));
+            kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, A.rho) : -wgt);
+        }
+        return make_float2(sum, -comp);
+    }
+    for (int qq = q0; qq <= (r.w1 - 1) >> 5; ++qq) {
         const int lo = max(r.w0 - 32 * qq, 0), hi = min(r.w1 - 32 * qq, 32);
         const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
         const uint32_t pv = __ldg(prow + qq), tv = __ldg(trow + qq);
