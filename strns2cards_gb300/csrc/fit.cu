@@ -219,7 +219,31 @@ __device__ __forceinline__ void fit_window_row(const FitArgs& a, const FitSmem& 
     const uint32_t* prow = S.pplane + th * a.WQ;
     const uint32_t* trow = S.tplane + th * a.WQ;
     const float dy = __fsub_rn(__fadd_rn((float)th, 0.5f), P.fy);
-    for (int qq = P.w0 >> 5; qq <= (P.w1 - 1) >> 5; ++qq) {
+    const int q0 = P.w0 >> 5, width = P.w1 - P.w0;
+    if (width <= 32) {
+        // the row as one 32-bit mask from w0 (one flat pixel loop, as aa_window_row)
+        const int sh = P.w0 & 31;
+        uint64_t pv = prow[q0], tv = trow[q0];
+        if (sh + width > 32) {
+            pv |= (uint64_t)prow[q0 + 1] << 32;
+            tv |= (uint64_t)trow[q0 + 1] << 32;
+        }
+        const uint32_t m = width == 32 ? 0xffffffffu : (1u << width) - 1u;
+        const uint32_t pw = (uint32_t)(pv >> sh) & m, tw = (uint32_t)(tv >> sh) & m;
+        const uint32_t pos = pw & ~tw;
+        uint32_t any = pw ^ tw;
+        while (any) {
+            const int bit = __ffs(any) - 1;
+            any &= any - 1;
+            const float dx = __fsub_rn(__fadd_rn((float)(P.w0 + bit), 0.5f), P.fx);
+            const float n2 = __fmaf_rn(dx, dx, __fmul_rn(dy, dy));
+            if (!(n2 < q.kr2)) continue;
+            const float wgt = __fmul_rn(q.cc, expf(-q.alpha * n2));
+            kahan_add(sum, comp, ((pos >> bit) & 1u) ? __fmul_rn(wgt, a.rho) : -wgt);
+        }
+        return;
+    }
+    for (int qq = q0; qq <= (P.w1 - 1) >> 5; ++qq) {
         const int lo = max(P.w0 - 32 * qq, 0), hi = min(P.w1 - 32 * qq, 32);
         const uint32_t m = (hi == 32 ? 0xffffffffu : ((1u << hi) - 1u)) & ~((1u << lo) - 1u);
         const uint32_t pv = prow[qq], tv = trow[qq];
@@ -450,7 +474,7 @@ __device__ void fit_tail(const FitArgs& a, const FitSmem& S, int c, int* s_misc,
     for (int v = tid; v < a.Vc; v += nt) cp[v] = make_float4(src[3 * v], src[3 * v + 1], src[3 * v + 2], S.P[v].w);
 }
 
-__global__ void fit_kernel(FitArgs a) {
+__global__ void __launch_bounds__(1024) fit_kernel(FitArgs a) {
     extern __shared__ __align__(16) unsigned char fit_smem[];
     __shared__ int s_item, s_last;
     __shared__ int s_misc[40];
