@@ -198,6 +198,10 @@ __device__ __forceinline__ int divmod_small(int local, int w, int& r) {
 }
 
 constexpr int kRasterChunk = 1024;
+// pixels of one bounding-box row per work unit (the triangle's corners loaded once for all):
+// 2 -> 4 took the config-2 card raster from 0.388 to 0.367 ms; 8 was slower (0.419 ms: the
+// thin cards' boxes leave more of each run outside)
+constexpr int kRasterRun = 4;
 
 // Balanced pass: warps take equal chunks of the global bbox-pixel index space.  A warp
 // keeps a window of 32 consecutive triangles' prefix values in its lanes, slides it along
@@ -273,22 +277,23 @@ __global__ void __launch_bounds__(256, 4) tri_fused_kernel(FusedRaster F) {
             }
             const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
             if (j < end) {
-                // work unit j: a pair of horizontally adjacent bounding-box pixels (the
-                // triangle's corners are loaded once for both)
+                // work unit j: a run of kRasterRun horizontally adjacent bounding-box pixels
+                // (the triangle's corners are loaded once for all of them)
                 const int64_t o = t0 + ow;
                 const int ob = (int)F.R.divT.div((uint32_t)o);
                 const int ot = (int)o - ob * F.R.T;
                 const int4 rc = F.rects[o];
                 const int local = (int)(j - (ow > 0 ? prev : start));
-                const int wp = (rc.w + 1) >> 1;
+                const int wp = (rc.w + (kRasterRun - 1)) / kRasterRun;
                 int r;
                 const int q = divmod_small(local, wp, r);
-                const int x = rc.z + 2 * r, y = rc.x + q;
+                const int x = rc.z + kRasterRun * r, y = rc.x + q;
                 float4 P0, P1, P2;
                 // only the bounding box's own pixels, as the list path tests
                 if (q < rc.y && y >= 0 && y < F.H && raster_corners(F, ob, ot, P0, P1, P2)) {
-                    raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x, y);
-                    if (2 * r + 1 < rc.w) raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x + 1, y);
+#pragma unroll
+                    for (int u = 0; u < kRasterRun; ++u)
+                        if (kRasterRun * r + u < rc.w) raster_covered(F, px_lut, py_lut, ob, ot, P0, P1, P2, x + u, y);
                 }
             }
             base = end;
@@ -320,8 +325,8 @@ __global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B,
         const int t = (int)idx - b * R.T;
         const int4 rc = tri_rect(H, W, R, b, t);
         rects[idx] = rc;
-        // work units of the balanced raster: pairs of horizontally adjacent pixels per row
-        areas[idx] = (int32_t)((uint32_t)rc.y * (((uint32_t)rc.w + 1u) >> 1));
+        // work units of the balanced raster: runs of kRasterRun horizontally adjacent pixels
+        areas[idx] = (int32_t)((uint32_t)rc.y * (((uint32_t)rc.w + (kRasterRun - 1)) / kRasterRun));
         if (CR.r && rc.y > 0 && rc.w > 0 && t < CR.num_t2c) {
             const int c = __ldg(CR.t2c + t);   // the raster's cluster bit for t (raster_covered)
             if (c >= 0 && c < CR.Kp) {
