@@ -177,6 +177,23 @@ S2C_API s2c_status s2c_compute_fragments(int H, int W, int B, int V, const float
                                          const int32_t* rects, int64_t num_frags, int32_t* frag_pix,
                                          float* frag_attrs, s2c_stream stream);
 
+/* new: the compacted fragment list -- what s2c_filter_valid_fragments leaves of
+ * s2c_compute_fragments' list, same order and values -- without the raw list.
+ * count_fragments (after s2c_compute_triangle_rects, num_bbox_pixels = its count) marks the
+ * covered bounding-box pixels in the workspace (16-byte aligned, count_fragments_workspace_size
+ * bytes) and returns their number in *num_frags (host; synchronises the stream);
+ * write_fragments, on the same stream with the same workspace, writes them into
+ * frag_pix (num_frags, 3) / frag_attrs (num_frags, 4, 16-byte aligned). */
+S2C_API size_t s2c_count_fragments_workspace_size(int64_t num_bbox_pixels);
+S2C_API s2c_status s2c_count_fragments(int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
+                                       const int32_t* prefix, const int32_t* rects, int64_t num_bbox_pixels,
+                                       void* workspace, size_t workspace_bytes, int64_t* num_frags,
+                                       s2c_stream stream);
+S2C_API s2c_status s2c_write_fragments(int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
+                                       const int32_t* prefix, const int32_t* rects, int64_t num_bbox_pixels,
+                                       const void* workspace, size_t workspace_bytes, int32_t* frag_pix,
+                                       float* frag_attrs, s2c_stream stream);
+
 /* replaces: depth_test (pystrns2cards.cpp:328-356; rasterize.cu:198-278).
  * rast_out (B, H, W, 4) must be zeroed by the caller (as rasterize.py:55-95 does); pixels
  * with fragments get the attributes of the nearest one (ties: first in fragment order). */

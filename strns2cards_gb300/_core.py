@@ -163,6 +163,32 @@ def compute_fragments(H, W, pos, tri, frag_prefix_sum, triangle_rects, frag_pix,
          ptr(triangle_rects), F, ptr(frag_pix), ptr(frag_attrs), _stream(pos))
 
 
+def compact_fragments(H, W, pos, tri, frag_prefix_sum, triangle_rects, num_bbox_pixels):
+    """The compacted fragment list (``filter_valid_fragments`` of ``compute_fragments``'s raw
+    list, same order and values) in two passes without the raw list: (frag_pix, frag_attrs)."""
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(tri, _i32, 2, 3, "tri")
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _arr(triangle_rects, _i32, 2, 4, "triangle_rects")
+    _cuda(pos, tri, frag_prefix_sum, triangle_rects, msg="All tensors must be CUDA tensors (device_id >= 0).")
+    B, V, _ = pos.shape
+    T = tri.shape[0]
+    if frag_prefix_sum.shape[0] != B * T or triangle_rects.shape[0] != B * T:
+        raise RuntimeError("Mismatch in prefix sum or rectangle count.")
+    F = int(num_bbox_pixels)
+    ws = workspace(_lib.lib().s2c_count_fragments_workspace_size(F), pos.device)
+    n = _lib.i64_out()
+    args = (int(H), int(W), B, V, ptr(pos), T, ptr(tri), ptr(frag_prefix_sum), ptr(triangle_rects), F, ptr(ws),
+            ws.numel())
+    call("s2c_count_fragments", *args, ctypes.byref(n), _stream(pos))
+    N = int(n.value)
+    frag_pix = torch.empty((N, 3), dtype=torch.int32, device=pos.device)
+    frag_attrs = torch.empty((N, 4), dtype=torch.float32, device=pos.device)
+    if N:
+        call("s2c_write_fragments", *args, ptr(frag_pix), ptr(frag_attrs), _stream(pos))
+    return frag_pix, frag_attrs
+
+
 def depth_test(H, W, frag_pix, frag_attrs, rast_out) -> None:
     _arr(frag_pix, _i32, 2, 3, "frag_pix")
     _arr(frag_attrs, _f32, 2, 4, "frag_attrs")

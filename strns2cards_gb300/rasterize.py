@@ -33,13 +33,10 @@ def compute_fragments(
     rects = torch.empty((B * T, 4), dtype=torch.int32, device=dev)
     prefix = torch.empty((B * T,), dtype=torch.int32, device=dev)
     F = _core.compute_triangle_rects(H, W, pos, tri, rects, prefix)
-    frag_pix = torch.full((F, 3), -1, dtype=torch.int32, device=dev)
-    frag_attrs = torch.empty((F, 4), dtype=torch.float32, device=dev)
-    _core.compute_fragments(H, W, pos, tri, prefix, rects, frag_pix, frag_attrs)
-    pix_out = torch.empty_like(frag_pix)
-    attrs_out = torch.empty_like(frag_attrs)
-    n = _core.filter_valid_fragments(frag_pix, frag_attrs, pix_out, attrs_out)
-    return pix_out[:n], attrs_out[:n]
+    # the reference lists every bounding-box pixel (-1 where uncovered) and compacts the list
+    # (rasterize.py:33-53); here the covered pixels are counted and written straight into a
+    # list of their own: the same fragments in the same order
+    return _core.compact_fragments(H, W, pos, tri, prefix, rects, F)
 
 
 def depth_test(B: int, resolution: Tuple[int, int], frag_pix: torch.Tensor, frag_attrs: torch.Tensor) -> torch.Tensor:

@@ -327,3 +327,38 @@ def test_rasterize_fused_rows_on_hard_triangles():
     assert torch.equal(fbits, ref_bits)
     assert torch.equal(frast, rast)
     assert int((rast[..., 3] > 0).sum()) > 1000
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_compacted_fragments_equal_the_filtered_raw_list(seed):
+    """``compute_fragments`` writes the covered pixels straight into their own list (a coverage
+    bit per bounding-box pixel, a scan, a write pass); it must equal the reference's way --
+    the raw list of every bounding-box pixel (-1 where uncovered) compacted by
+    ``filter_valid_fragments`` -- value for value and in order, including triangles with
+    empty, off-screen, degenerate and huge boxes, several views and an empty input."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    rng = np.random.default_rng(seed)
+    B, H, W, V, T = 3, 83, 150, 500, 700
+    pos = rng.uniform(-1.3, 1.3, size=(B, V, 4)).astype(np.float32)
+    pos[..., 3] = rng.uniform(0.4, 1.6, size=(B, V))
+    pos[..., :2] *= pos[..., 3:4]
+    pos[..., 2] = rng.uniform(-0.8, 0.8, size=(B, V)) * pos[..., 3]
+    pos[:, :40, :2] *= 40.0                                    # far beyond the view
+    tri = rng.integers(0, V, size=(T, 3)).astype(np.int32)
+    tri[:50, 1] = tri[:50, 0]                                  # degenerate
+    tri[50:60] = rng.integers(0, 40, size=(10, 3))             # huge boxes
+    p, t = cu(pos), cu(tri)
+    rects = torch.empty((B * T, 4), dtype=torch.int32, device="cuda")
+    prefix = torch.empty(B * T, dtype=torch.int32, device="cuda")
+    F = _core.compute_triangle_rects(H, W, p, t, rects, prefix)
+    raw_p = torch.full((F, 3), -1, dtype=torch.int32, device="cuda")
+    raw_a = torch.empty((F, 4), dtype=torch.float32, device="cuda")
+    _core.compute_fragments(H, W, p, t, prefix, rects, raw_p, raw_a)
+    out_p, out_a = torch.empty_like(raw_p), torch.empty_like(raw_a)
+    n = _core.filter_valid_fragments(raw_p, raw_a, out_p, out_a)
+    fp, fa = s2c.compute_fragments((H, W), p, t)
+    assert fp.shape[0] == n > 1000
+    assert torch.equal(fp, out_p[:n]) and torch.equal(fa, out_a[:n])
+    ep, ea = s2c.compute_fragments((H, W), p, t[:0])
+    assert ep.shape == (0, 3) and ea.shape == (0, 4)
