@@ -142,20 +142,93 @@ s2c_status launch_curves(bool skin, int N, int V, const float* x, const float* a
 }
 
 // Arclength resampling of ragged strands (the reference's host resample_strands_by_arclength,
-// hair_loader.cpp:261-307), one thread per strand with the same FP32 operations in the same
-// order: bit-identical to the host version.  ends = inclusive prefix of the point counts.
-__global__ void resample_kernel(int ns, const int32_t* __restrict__ counts, const int32_t* __restrict__ ends,
-                                const float* __restrict__ pts, int64_t npts, int T, float* __restrict__ len,
-                                float* __restrict__ out, int32_t* __restrict__ bad) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += gridDim.x * blockDim.x) {
+// hair_loader.cpp:261-307) with the same FP32 operations in the same order per strand:
+// bit-identical to the host version.  ends = inclusive prefix of the point counts.
+// The same per strand with a warp: the strand's points are read into shared memory with
+// coalesced loads, the lanes take the segment lengths, one lane runs the cumulative sum in
+// order (the host's summation order, so the arclengths are bit-identical), the lanes
+// normalise and take the output samples.  Strands longer than kResampleCap points go to
+// resample_kernel (its thread per strand works from global memory).
+constexpr int kResampleCap = 384, kResampleWarps = 4;
+
+__global__ void __launch_bounds__(32 * kResampleWarps) resample_warp_kernel(
+    int ns, const int32_t* __restrict__ counts, const int32_t* __restrict__ ends, const float* __restrict__ pts,
+    int64_t npts, int T, float* __restrict__ out, int32_t* __restrict__ long_list, int32_t* __restrict__ n_long,
+    int32_t* __restrict__ bad) {
+    __shared__ float s_p[kResampleWarps][3 * kResampleCap];
+    __shared__ float s_L[kResampleWarps][kResampleCap];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    float* P = s_p[w];
+    float* L = s_L[w];
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (int i = gw; i < ns; i += nw) {
         const int N = counts[i];
         const int64_t at = (int64_t)ends[i] - N;
         float* o = out + (int64_t)i * T * 3;
         if (N < 2 || at < 0 || at + N > npts) {   // too short, or counts overrunning the points
-            atomicMax(bad, 1);
-            for (int k = 0; k < 3 * T; ++k) o[k] = __int_as_float(0x7fc00000);
+            if (lane == 0) atomicMax(bad, 1);
+            for (int k = lane; k < 3 * T; k += 32) o[k] = __int_as_float(0x7fc00000);
             continue;
         }
+        if (N > kResampleCap) {
+            if (lane == 0) long_list[atomicAdd(n_long, 1)] = i;
+            continue;
+        }
+        const float* p = pts + 3 * at;
+        for (int k = lane; k < 3 * N; k += 32) P[k] = __ldg(p + k);
+        __syncwarp();
+        for (int j = 1 + lane; j < N; j += 32) {
+            const float dx = __fsub_rn(P[3 * j], P[3 * j - 3]);
+            const float dy = __fsub_rn(P[3 * j + 1], P[3 * j - 2]);
+            const float dz = __fsub_rn(P[3 * j + 2], P[3 * j - 1]);
+            L[j] = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        }
+        __syncwarp();
+        if (lane == 0) {
+            float acc = 0.f;
+            L[0] = 0.f;
+            for (int j = 1; j < N; ++j) {
+                acc = __fadd_rn(acc, L[j]);
+                L[j] = acc;
+            }
+        }
+        __syncwarp();
+        const float total = L[N - 1];
+        __syncwarp();
+        for (int j = lane; j < N; j += 32) L[j] = __fdiv_rn(L[j], total);
+        __syncwarp();
+        for (int j = lane; j + 1 < T; j += 32) {
+            const float t = __fdiv_rn((float)j, (float)(T - 1));
+            int lo = 0, hi = N;   // first index with L > t
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (!(t < L[mid])) lo = mid + 1;
+                else hi = mid;
+            }
+            const int k = min(max(lo, 1), N - 1);
+            const float den = __fsub_rn(L[k], L[k - 1]);
+            const float t0 = __fdiv_rn(__fsub_rn(L[k], t), den);
+            const float t1 = __fdiv_rn(__fsub_rn(t, L[k - 1]), den);
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                o[3 * j + c] = __fadd_rn(__fmul_rn(t0, P[3 * (k - 1) + c]), __fmul_rn(t1, P[3 * k + c]));
+        }
+        if (lane < 3) o[3 * (T - 1) + lane] = P[3 * (N - 1) + lane];
+        __syncwarp();
+    }
+}
+
+// the strands resample_warp_kernel left (longer than kResampleCap points): a thread each
+__global__ void resample_long_kernel(const int32_t* __restrict__ long_list, const int32_t* __restrict__ n_long,
+                                     const int32_t* __restrict__ counts, const int32_t* __restrict__ ends,
+                                     const float* __restrict__ pts, int64_t npts, int T, float* __restrict__ len,
+                                     float* __restrict__ out) {
+    const int n = *n_long;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const int i = long_list[q];
+        const int N = counts[i];
+        const int64_t at = (int64_t)ends[i] - N;
+        float* o = out + (int64_t)i * T * 3;
         const float* p = pts + 3 * at;
         float* L = len + at;
         L[0] = 0.f;
@@ -170,7 +243,7 @@ __global__ void resample_kernel(int ns, const int32_t* __restrict__ counts, cons
         for (int j = 0; j < N; ++j) L[j] = __fdiv_rn(L[j], total);
         for (int j = 0; j + 1 < T; ++j) {
             const float t = __fdiv_rn((float)j, (float)(T - 1));
-            int lo = 0, hi = N;   // first index with L > t
+            int lo = 0, hi = N;
             while (lo < hi) {
                 const int mid = (lo + hi) >> 1;
                 if (!(t < L[mid])) lo = mid + 1;
@@ -223,8 +296,8 @@ S2C_API s2c_status s2c_skinning(int N, int V, const float* strands, const float*
 
 extern "C" size_t s2c_resample_strands_workspace_size(int num_strands, int64_t num_points) {
     const size_t ns = (size_t)(num_strands > 0 ? num_strands : 1);
-    return s2c::align_up(ns * 4, 256) + s2c::align_up((size_t)(num_points > 0 ? num_points : 1) * 4, 256) + 256 +
-           s2c::align_up(s2c::scan_workspace_bytes(ns), 256) + 512;
+    return 2 * s2c::align_up(ns * 4, 256) + s2c::align_up((size_t)(num_points > 0 ? num_points : 1) * 4, 256) +
+           512 + s2c::align_up(s2c::scan_workspace_bytes(ns), 256) + 512;
 }
 
 extern "C" s2c_status s2c_resample_strands_by_arclength(int num_strands, const int32_t* num_samples,
@@ -239,17 +312,24 @@ extern "C" s2c_status s2c_resample_strands_by_arclength(int num_strands, const i
                 "resample_strands_by_arclength: workspace too small");
     s2c::Carver cv(workspace, workspace_bytes);
     int32_t* ends = cv.take<int32_t>(num_strands);
+    int32_t* long_list = cv.take<int32_t>(num_strands);
     float* len = cv.take<float>(num_points > 0 ? num_points : 1);
-    int32_t* bad = cv.take<int32_t>(1);
+    int32_t* flags = cv.take<int32_t>(2);   // [0] bad counts, [1] long strands
     void* scan = cv.take<char>(s2c::scan_workspace_bytes(num_strands));
     int64_t* tot = cv.take<int64_t>(1);
+    S2C_REQUIRE(cv.ok(), "resample_strands_by_arclength: workspace too small");
     cudaStream_t st = (cudaStream_t)stream;
     s2c_status s = s2c::inclusive_scan_i32(num_samples, num_strands, ends, scan, tot, st);
     if (s != S2C_OK) return s;
-    cudaError_t e = cudaMemsetAsync(bad, 0, 4, st);
+    cudaError_t e = cudaMemsetAsync(flags, 0, 8, st);
     if (e != cudaSuccess) return s2c::cuda_status(e, "resample_strands_by_arclength: memset");
-    s2c::resample_kernel<<<s2c::grid_for(num_strands, 128, (int64_t)s2c::num_sms() * 16), 128, 0, st>>>(
-        num_strands, num_samples, ends, points, num_points, target, len, out, bad);
-    S2C_CHECK_LAUNCH("resample_kernel");
+    constexpr int threads = 32 * s2c::kResampleWarps;
+    s2c::resample_warp_kernel<<<s2c::grid_for((int64_t)num_strands * 32, threads, (int64_t)s2c::num_sms() * 16),
+                                threads, 0, st>>>(num_strands, num_samples, ends, points, num_points, target, out,
+                                                  long_list, flags + 1, flags);
+    S2C_CHECK_LAUNCH("resample_warp_kernel");
+    s2c::resample_long_kernel<<<s2c::num_sms() * 2, 128, 0, st>>>(long_list, flags + 1, num_samples, ends, points,
+                                                                    num_points, target, len, out);
+    S2C_CHECK_LAUNCH("resample_long_kernel");
     return S2C_OK;
 }

@@ -105,10 +105,13 @@ def test_curves_empty_and_errors():
 
 def test_device_resampling_equals_host():
     """Ragged strands resampled on the device equal the host version bit for bit (the same
-    FP32 operations in the same order); strands too short give NaN rows."""
+    FP32 operations in the same order), for strands a warp takes through shared memory and
+    for strands longer than that (up to 1,500 points, a thread each); strands too short give
+    NaN rows."""
     import strns2cards_gb300 as s2c
     rng = np.random.default_rng(9)
     counts = rng.integers(2, 300, size=5000).astype(np.int32)
+    counts[::97] = rng.integers(380, 1500, size=counts[::97].shape[0])
     pts = np.cumsum(rng.normal(scale=0.02, size=(int(counts.sum()), 3)), 0).astype(np.float32)
     for T in (2, 33, 100):
         host = s2c.resample_strands_by_arclength(counts, pts, T)
