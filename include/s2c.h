@@ -74,6 +74,24 @@ S2C_API s2c_status s2c_dda_compute_fragments(int64_t num_prims, int64_t num_frag
                                      const int32_t* edges, int32_t* frag_pix,
                                      float* frag_attrs, s2c_stream stream);
 
+/* new: the compacted list -- what s2c_filter_valid_fragments leaves of
+ * s2c_dda_compute_fragments' list, same order and values -- without the raw list (as
+ * s2c_count_fragments / s2c_write_fragments for triangles): count after s2c_dda_compute_span
+ * (num_steps = its count; *num_frags on the host, synchronising), then write on the same
+ * stream with the same workspace (16-byte aligned). */
+S2C_API size_t s2c_dda_count_fragments_workspace_size(int64_t num_steps);
+S2C_API s2c_status s2c_dda_count_fragments(int64_t num_prims, int64_t num_steps, const int32_t* frag_prefix_sum,
+                                           const int32_t* edge_ids, const float* frag_slopes,
+                                           const float* frag_spans, int H, int W, int B, int V, const float* pos,
+                                           int E, const int32_t* edges, void* workspace, size_t workspace_bytes,
+                                           int64_t* num_frags, s2c_stream stream);
+S2C_API s2c_status s2c_dda_write_fragments(int64_t num_prims, int64_t num_steps, const int32_t* frag_prefix_sum,
+                                           const int32_t* edge_ids, const float* frag_slopes,
+                                           const float* frag_spans, int H, int W, int B, int V, const float* pos,
+                                           int E, const int32_t* edges, const void* workspace,
+                                           size_t workspace_bytes, int32_t* frag_pix, float* frag_attrs,
+                                           s2c_stream stream);
+
 /* replaces: filter_valid_fragments (pystrns2cards.cpp:358-392; rasterize.cu:280-365).
  * Keeps fragments with frag_pix[i,0] >= 0 in their original order (the reference's order
  * depends on block scheduling); the kept count goes to *num_valid (host, synchronising). */

@@ -91,6 +91,34 @@ def dda_compute_fragments(frag_prefix_sum, edge_ids, frag_slopes, frag_spans, H,
          int(H), int(W), B, V, ptr(pos), edges.shape[0], ptr(edges), ptr(frag_pix), ptr(frag_attrs), _stream(pos))
 
 
+def dda_compact_fragments(frag_prefix_sum, edge_ids, frag_slopes, frag_spans, H, W, pos, edges, num_steps):
+    """The compacted DDA fragment list (``filter_valid_fragments`` of ``dda_compute_fragments``'s
+    raw list, same order and values) in two passes without the raw list: (frag_pix, frag_attrs)."""
+    _arr(frag_prefix_sum, _i32, 1, name="frag_prefix_sum")
+    _arr(edge_ids, _i32, 1, name="edge_ids")
+    _arr(frag_slopes, _f32, 2, 2, "frag_slopes")
+    _arr(frag_spans, _f32, 2, 4, "frag_spans")
+    _arr(pos, _f32, 3, 4, "pos")
+    _arr(edges, _i32, 2, 2, "edges")
+    _cuda(frag_prefix_sum, edge_ids, frag_slopes, frag_spans, pos, edges)
+    P = edge_ids.shape[0]
+    if frag_prefix_sum.shape[0] != P or frag_slopes.shape[0] != P or frag_spans.shape[0] != P:
+        raise RuntimeError("Invalid shape for input arrays.")
+    B, V, _ = pos.shape
+    F = int(num_steps)
+    ws = workspace(_lib.lib().s2c_dda_count_fragments_workspace_size(F), pos.device)
+    args = (P, F, ptr(frag_prefix_sum), ptr(edge_ids), ptr(frag_slopes), ptr(frag_spans), int(H), int(W), B, V,
+            ptr(pos), edges.shape[0], ptr(edges), ptr(ws), ws.numel())
+    n = _lib.i64_out()
+    call("s2c_dda_count_fragments", *args, ctypes.byref(n), _stream(pos))
+    N = int(n.value)
+    frag_pix = torch.empty((N, 3), dtype=torch.int32, device=pos.device)
+    frag_attrs = torch.empty((N, 4), dtype=torch.float32, device=pos.device)
+    if N:
+        call("s2c_dda_write_fragments", *args, ptr(frag_pix), ptr(frag_attrs), _stream(pos))
+    return frag_pix, frag_attrs
+
+
 # ---- fragments (pystrns2cards.cpp:358-392, 440-478) ----------------------------------
 def filter_valid_fragments(frag_pix, frag_attrs, frag_pix_out, frag_attrs_out) -> int:
     for t, d, last, nm in ((frag_pix, _i32, 3, "frag_pix"), (frag_attrs, _f32, 4, "frag_attrs"),

@@ -44,6 +44,10 @@ SIGNATURES = {
     "s2c_compute_triangle_rects_workspace_size": ([c_i, c_i], c_sz),
     "s2c_compute_triangle_rects": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, vp, c_sz, i64p, vp], c_i),
     "s2c_compute_fragments": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i64, vp, vp, vp], c_i),
+    "s2c_dda_count_fragments_workspace_size": ([c_i64], c_sz),
+    "s2c_dda_count_fragments": ([c_i64, c_i64, vp, vp, vp, vp, c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_sz, i64p, vp], c_i),
+    "s2c_dda_write_fragments": ([c_i64, c_i64, vp, vp, vp, vp, c_i, c_i, c_i, c_i, vp, c_i, vp, vp, c_sz, vp, vp, vp],
+                                c_i),
     "s2c_count_fragments_workspace_size": ([c_i64], c_sz),
     "s2c_count_fragments": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i64, vp, c_sz, i64p, vp], c_i),
     "s2c_write_fragments": ([c_i, c_i, c_i, c_i, vp, c_i, vp, vp, vp, c_i64, vp, c_sz, vp, vp, vp], c_i),

@@ -7,6 +7,7 @@
 
 #include "lines.cuh"
 #include "scan.cuh"
+#include "list.cuh"
 
 namespace s2c {
 
@@ -70,6 +71,60 @@ __global__ void __launch_bounds__(256) dda_fragments_kernel(int64_t P, int64_t F
     frag_pix[3 * idx + 1] = h;
     frag_pix[3 * idx + 2] = w;
     frag_attrs[idx] = make_float4(s.axis, t1, z, (float)(q.e + 1));
+}
+
+// The compacted fragment list (what filter_valid_fragments leaves of dda_fragments_kernel's
+// list, same order and values) in two passes over the same DDA step index space (list.cuh).
+template <bool kWrite>
+__global__ void __launch_bounds__(256) dda_list_kernel(int64_t P, uint32_t F, const int32_t* __restrict__ prefix,
+                                                       Lines L, const float2* __restrict__ slopes,
+                                                       const float4* __restrict__ spans, int H, int W,
+                                                       uint32_t* __restrict__ mask, const int32_t* __restrict__ wpre,
+                                                       int32_t* __restrict__ frag_pix,
+                                                       float4* __restrict__ frag_attrs) {
+    // step k of primitive o, accepted: (b, h, w) and (axis, t1, z, e + 1)
+    auto step = [&](int64_t o, int k, int& h, int& w, float& axis, float& t1, float& z, Prim& q) {
+        const float2 sl = __ldg(slopes + o);
+        const float4 sp = __ldg(spans + o);
+        Span s;
+        s.axis = sl.x;
+        s.slope = sl.y;
+        s.sx = sp.x;
+        s.sy = sp.y;
+        s.off0 = sp.z;
+        s.off1 = sp.w;
+        s.count = 0;
+        float x, y;
+        dda_sample(s, k, x, y);
+        h = f2i(floorf(y));
+        w = f2i(floorf(x));
+        if (h < 0 || h >= H || w < 0 || w >= W) return false;
+        if (!load_prim(o, L, q)) return false;
+        axis = s.axis;
+        t1 = dda_t1(q.p0, q.p1, x, y, s.axis, H, W);
+        z = dda_z(q.p0, q.p1, t1);
+        return z_ok(z);
+    };
+    list_pass<kWrite>(
+        P, F, prefix, mask, wpre,
+        [&](int64_t o, int k) {
+            int h, w;
+            float axis, t1, z;
+            Prim q;
+            return step(o, k, h, w, axis, t1, z, q);
+        },
+        [&](int64_t o, int k, int64_t at) {
+            int h = 0, w = 0;
+            float axis = 0.f, t1 = 0.f, z = 0.f;
+            Prim q;
+            q.b = 0;
+            q.e = 0;
+            step(o, k, h, w, axis, t1, z, q);   // accepted in pass 1: the same values again
+            frag_pix[3 * at] = q.b;
+            frag_pix[3 * at + 1] = h;
+            frag_pix[3 * at + 2] = w;
+            frag_attrs[at] = make_float4(axis, t1, z, (float)(q.e + 1));
+        });
 }
 
 // rasterize.cu:474-498 (bounds-checked: invalid views, pixels, prims or clusters are skipped)
@@ -152,6 +207,62 @@ extern "C" s2c_status s2c_dda_compute_fragments(int64_t P, int64_t F, const int3
         P, F, prefix, make_lines(edge_ids, B, V, pos, E, edges), (const float2*)slopes, (const float4*)spans, H, W,
         frag_pix, (float4*)frag_attrs);
     S2C_CHECK_LAUNCH("dda_fragments_kernel");
+    return S2C_OK;
+}
+
+extern "C" size_t s2c_dda_count_fragments_workspace_size(int64_t num_steps) {
+    return list_carve(num_steps < 0 ? 0 : num_steps, nullptr, (size_t)-1, nullptr) + 256;
+}
+
+static s2c_status dda_list_args(const char* who, int64_t P, int64_t F, const int32_t* prefix, const int32_t* edge_ids,
+                                const float* slopes, const float* spans, int H, int W, int B, int V, const float* pos,
+                                int E, const int32_t* edges, void* ws, size_t ws_bytes, ListWs& w) {
+    if (s2c_status s = check_lines(P, edge_ids, H, W, B, V, pos, E, edges, who)) return s;
+    S2C_REQUIRE(F >= 0 && F <= 0x7fffffffLL, "%s: fragment count out of range", who);
+    S2C_REQUIRE(F == 0 || (prefix && slopes && spans), "%s: null pointer", who);
+    S2C_REQUIRE(((uintptr_t)spans & 15) == 0 && ((uintptr_t)slopes & 7) == 0, "%s: misaligned span/slope arrays", who);
+    S2C_REQUIRE(ws && ((uintptr_t)ws & 15) == 0, "%s: null or misaligned workspace", who);
+    const size_t need = list_carve(F, ws, ws_bytes, &w);
+    S2C_REQUIRE(need <= ws_bytes, "%s: workspace of %zu bytes, need %zu", who, ws_bytes, need);
+    return S2C_OK;
+}
+
+extern "C" s2c_status s2c_dda_count_fragments(int64_t P, int64_t F, const int32_t* prefix, const int32_t* edge_ids,
+                                              const float* slopes, const float* spans, int H, int W, int B, int V,
+                                              const float* pos, int E, const int32_t* edges, void* workspace,
+                                              size_t workspace_bytes, int64_t* num_frags, s2c_stream stream) {
+    ListWs w;
+    if (s2c_status s = dda_list_args("dda_count_fragments", P, F, prefix, edge_ids, slopes, spans, H, W, B, V, pos,
+                                     E, edges, workspace, workspace_bytes, w))
+        return s;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(w.mask, 0, (size_t)std::max<int64_t>((F + 31) / 32, 1) * 4, st);
+    if (e != cudaSuccess) return cuda_status(e, "dda_count_fragments: memset");
+    if (F > 0 && P > 0) {
+        dda_list_kernel<false><<<list_grid(F), 256, 0, st>>>(P, (uint32_t)F, prefix,
+                                                            make_lines(edge_ids, B, V, pos, E, edges),
+                                                            (const float2*)slopes, (const float4*)spans, H, W,
+                                                            w.mask, nullptr, nullptr, nullptr);
+        S2C_CHECK_LAUNCH("dda_list_kernel<count>");
+    }
+    return list_count(P > 0 ? F : 0, w, num_frags, st);
+}
+
+extern "C" s2c_status s2c_dda_write_fragments(int64_t P, int64_t F, const int32_t* prefix, const int32_t* edge_ids,
+                                              const float* slopes, const float* spans, int H, int W, int B, int V,
+                                              const float* pos, int E, const int32_t* edges, const void* workspace,
+                                              size_t workspace_bytes, int32_t* frag_pix, float* frag_attrs,
+                                              s2c_stream stream) {
+    ListWs w;
+    if (s2c_status s = dda_list_args("dda_write_fragments", P, F, prefix, edge_ids, slopes, spans, H, W, B, V, pos,
+                                     E, edges, const_cast<void*>(workspace), workspace_bytes, w))
+        return s;
+    if (F == 0 || P == 0) return S2C_OK;
+    S2C_REQUIRE(frag_pix && frag_attrs && ((uintptr_t)frag_attrs & 15) == 0, "dda_write_fragments: bad outputs");
+    dda_list_kernel<true><<<list_grid(F), 256, 0, (cudaStream_t)stream>>>(
+        P, (uint32_t)F, prefix, make_lines(edge_ids, B, V, pos, E, edges), (const float2*)slopes,
+        (const float4*)spans, H, W, w.mask, w.wpre, frag_pix, (float4*)frag_attrs);
+    S2C_CHECK_LAUNCH("dda_list_kernel<write>");
     return S2C_OK;
 }
 

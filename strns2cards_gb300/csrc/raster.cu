@@ -11,6 +11,7 @@
 
 #include "common.cuh"
 #include "scan.cuh"
+#include "list.cuh"
 #include "tri.cuh"
 
 namespace s2c {
@@ -197,106 +198,47 @@ __device__ __forceinline__ int divmod_small(int local, int w, int& r) {
     return q;
 }
 
-// The compacted fragment list (what filter_valid_fragments leaves of tri_fragments_kernel's list) in two
-// passes over the same bounding-box pixel index space, without the raw list: pass 1 sets one
-// coverage bit per raw index, a scan of the bit words' popcounts places every covered pixel,
-// pass 2 writes it there.  Warps take 1024-index chunks and keep a window of 32 consecutive
-// triangles' prefix values in their lanes (the owner of a lane's index by a 5-step shuffle
-// search), as the fused raster does, instead of a binary search per pixel.
-constexpr int kListChunk = 1024;   // a multiple of 32: a mask word never straddles two chunks
-
+// The compacted fragment list (what filter_valid_fragments leaves of tri_fragments_kernel's
+// list) in two passes over the same bounding-box pixel index space (list.cuh).
 template <bool kWrite>
 __global__ void __launch_bounds__(256) tri_list_kernel(int H, int W, Tris R, int64_t BT, uint32_t F,
                                                        const int32_t* __restrict__ prefix,
                                                        const int4* __restrict__ rects, uint32_t* __restrict__ mask,
                                                        const int32_t* __restrict__ wpre, int32_t* __restrict__ frag_pix,
                                                        float4* __restrict__ frag_attrs) {
-    const int lane = threadIdx.x & 31;
-    const int64_t warp0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int64_t nch = ((int64_t)F + kListChunk - 1) / kListChunk;
-    for (int64_t ch = warp0; ch < nch; ch += nwarps) {
-        const uint32_t c0 = (uint32_t)(ch * kListChunk);
-        const uint32_t c1 = (uint32_t)min((int64_t)F, (ch + 1) * kListChunk);
-        int64_t lo = 0, hi = BT;
-        while (lo < hi) {
-            const int64_t mid = (lo + hi) >> 1;
-            if ((uint32_t)__ldg(prefix + mid) <= c0) lo = mid + 1;
-            else hi = mid;
-        }
-        int64_t t0 = lo;
-        uint32_t start = t0 > 0 ? (uint32_t)__ldg(prefix + t0 - 1) : 0u;
-        uint32_t pre = t0 + lane < BT ? (uint32_t)__ldg(prefix + t0 + lane) : 0xffffffffu;
-        uint32_t base = c0;
-        while (base < c1) {
-            for (;;) {
-                const unsigned m = __ballot_sync(0xffffffffu, pre <= base);
-                if (!m) break;
-                const int adv = __popc(m);
-                start = __shfl_sync(0xffffffffu, pre, adv - 1);
-                t0 += adv;
-                pre = t0 + lane < BT ? (uint32_t)__ldg(prefix + t0 + lane) : 0xffffffffu;
-            }
-            const uint32_t wend = __shfl_sync(0xffffffffu, pre, 31);
-            const uint32_t end = min(min(c1, base + 32u), wend);
-            const uint32_t j = base + lane;
-            int ow = 0;
-#pragma unroll
-            for (int step = 16; step; step >>= 1) {
-                const uint32_t pv = __shfl_sync(0xffffffffu, pre, ow + step - 1);
-                if (pv <= j) ow += step;
-            }
-            const uint32_t prev = __shfl_sync(0xffffffffu, pre, ow > 0 ? ow - 1 : 0);
-            bool cov = false;
+    // pixel k of triangle o's box, covered: (b, y, x) and (b0, b1, z)
+    auto cover = [&](int64_t o, int k, int& b, int& t, int& x, int& y, float& b0, float& b1, float& z) {
+        b = (int)R.divT.div((uint32_t)o);
+        t = (int)o - b * R.T;
+        const int4 rc = __ldg(rects + o);
+        if (rc.w <= 0 || rc.y <= 0) return false;
+        int r;
+        const int q = divmod_small(k, rc.w, r);
+        y = rc.x + q;
+        x = rc.z + r;
+        if (x < 0 || x >= W || y < 0 || y >= H) return false;
+        const int i0 = __ldg(R.tri + 3 * t), i1 = __ldg(R.tri + 3 * t + 1), i2 = __ldg(R.tri + 3 * t + 2);
+        if ((unsigned)i0 >= (unsigned)R.V || (unsigned)i1 >= (unsigned)R.V || (unsigned)i2 >= (unsigned)R.V)
+            return false;
+        const float4* pb = R.pos4 + (int64_t)b * R.V;
+        return tri_cover(H, W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z);
+    };
+    list_pass<kWrite>(
+        BT, F, prefix, mask, wpre,
+        [&](int64_t o, int k) {
+            int b, t, x, y;
+            float b0, b1, z;
+            return cover(o, k, b, t, x, y, b0, b1, z);
+        },
+        [&](int64_t o, int k, int64_t at) {
             int b = 0, t = 0, x = 0, y = 0;
             float b0 = 0.f, b1 = 0.f, z = 0.f;
-            // pass 2 skips the pixels pass 1 left uncovered (j < end <= F: its word exists)
-            const bool look = j < end && (!kWrite || ((mask[j >> 5] >> (j & 31)) & 1u));
-            if (look) {
-                const int64_t o = t0 + ow;
-                b = (int)R.divT.div((uint32_t)o);
-                t = (int)o - b * R.T;
-                const int4 rc = __ldg(rects + o);
-                if (rc.w > 0 && rc.y > 0) {
-                    const int local = (int)(j - (ow > 0 ? prev : start));
-                    int r;
-                    const int q = divmod_small(local, rc.w, r);
-                    y = rc.x + q;
-                    x = rc.z + r;
-                    if (x >= 0 && x < W && y >= 0 && y < H) {
-                        const int i0 = __ldg(R.tri + 3 * t), i1 = __ldg(R.tri + 3 * t + 1),
-                                  i2 = __ldg(R.tri + 3 * t + 2);
-                        if ((unsigned)i0 < (unsigned)R.V && (unsigned)i1 < (unsigned)R.V && (unsigned)i2 < (unsigned)R.V) {
-                            const float4* pb = R.pos4 + (int64_t)b * R.V;
-                            cov = tri_cover(H, W, __ldg(pb + i0), __ldg(pb + i1), __ldg(pb + i2), x, y, b0, b1, z);
-                        }
-                    }
-                }
-            }
-            if (!kWrite) {
-                // lanes 0 .. end - base - 1 hold indices base .. end - 1
-                const unsigned m = __ballot_sync(0xffffffffu, cov);
-                if (lane == 0 && m) {
-                    const uint32_t w = base >> 5, sh = base & 31;
-                    atomicOr(mask + w, m << sh);
-                    if (sh && (m >> (32 - sh))) atomicOr(mask + w + 1, m >> (32 - sh));
-                }
-            } else if (cov) {
-                const uint32_t w = j >> 5;
-                const int64_t at = (int64_t)(w ? (uint32_t)wpre[w - 1] : 0u) + __popc(mask[w] & ((1u << (j & 31)) - 1u));
-                frag_pix[3 * at] = b;
-                frag_pix[3 * at + 1] = y;
-                frag_pix[3 * at + 2] = x;
-                frag_attrs[at] = make_float4(b0, b1, z, (float)(t + 1));
-            }
-            base = end;
-        }
-    }
-}
-
-__global__ void popc_words_kernel(int64_t n, const uint32_t* __restrict__ mask, int32_t* __restrict__ counts) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        counts[i] = __popc(mask[i]);
+            cover(o, k, b, t, x, y, b0, b1, z);   // accepted in pass 1: the same values again
+            frag_pix[3 * at] = b;
+            frag_pix[3 * at + 1] = y;
+            frag_pix[3 * at + 2] = x;
+            frag_attrs[at] = make_float4(b0, b1, z, (float)(t + 1));
+        });
 }
 
 
@@ -745,25 +687,6 @@ extern "C" s2c_status s2c_compute_fragments(int H, int W, int B, int V, const fl
 }
 
 namespace {
-struct ListWs {
-    uint32_t* mask;
-    int32_t* wpre;
-    int64_t* total;
-    void* scan;
-};
-
-size_t list_carve(int64_t F, void* base, size_t cap, ListWs* w) {
-    Carver cv(base, cap);
-    ListWs r;
-    const int64_t nw = std::max<int64_t>((F + 31) / 32, 1);
-    r.mask = cv.take<uint32_t>(nw);
-    r.wpre = cv.take<int32_t>(nw);
-    r.total = cv.take<int64_t>(1);
-    r.scan = cv.take<char>(scan_workspace_bytes(nw));
-    if (w) *w = r;
-    return cv.off;
-}
-
 s2c_status list_args(const char* what, int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
                      const int32_t* prefix, const int32_t* rects, int64_t F, void* ws, size_t ws_bytes, ListWs& w) {
     S2C_REQUIRE(H > 0 && W > 0 && B > 0 && V >= 0 && T >= 0 && F >= 0, "%s: bad sizes", what);
@@ -793,16 +716,12 @@ extern "C" s2c_status s2c_count_fragments(int H, int W, int B, int V, const floa
     cudaError_t e = cudaMemsetAsync(w.mask, 0, (size_t)std::max<int64_t>(nw, 1) * 4, st);
     if (e != cudaSuccess) return cuda_status(e, "count_fragments: memset");
     if (F > 0) {
-        const int64_t BT = (int64_t)B * T;
-        const unsigned grid = (unsigned)std::min<int64_t>((F + kListChunk - 1) / kListChunk / 8 + 1, (int64_t)num_sms() * 8);
-        tri_list_kernel<false><<<grid, 256, 0, st>>>(H, W, make_tris(V, pos, T, tri), BT, (uint32_t)F, prefix,
-                                                    (const int4*)rects, w.mask, nullptr, nullptr, nullptr);
+        tri_list_kernel<false><<<list_grid(F), 256, 0, st>>>(H, W, make_tris(V, pos, T, tri), (int64_t)B * T,
+                                                            (uint32_t)F, prefix, (const int4*)rects, w.mask, nullptr,
+                                                            nullptr, nullptr);
         S2C_CHECK_LAUNCH("tri_list_kernel<count>");
-        popc_words_kernel<<<grid_for(nw, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(nw, w.mask, w.wpre);
-        S2C_CHECK_LAUNCH("popc_words_kernel");
     }
-    if (s2c_status s = inclusive_scan_i32(w.wpre, nw, w.wpre, w.scan, w.total, st)) return s;
-    return read_count(w.total, num_frags, st);
+    return list_count(F, w, num_frags, st);
 }
 
 extern "C" s2c_status s2c_write_fragments(int H, int W, int B, int V, const float* pos, int T, const int32_t* tri,
@@ -816,8 +735,7 @@ extern "C" s2c_status s2c_write_fragments(int H, int W, int B, int V, const floa
     if (F == 0) return S2C_OK;
     S2C_REQUIRE(frag_pix && frag_attrs && ((uintptr_t)frag_attrs & 15) == 0, "write_fragments: bad outputs");
     cudaStream_t st = (cudaStream_t)stream;
-    const unsigned grid = (unsigned)std::min<int64_t>((F + kListChunk - 1) / kListChunk / 8 + 1, (int64_t)num_sms() * 8);
-    tri_list_kernel<true><<<grid, 256, 0, st>>>(H, W, make_tris(V, pos, T, tri), (int64_t)B * T, (uint32_t)F, prefix,
+    tri_list_kernel<true><<<list_grid(F), 256, 0, st>>>(H, W, make_tris(V, pos, T, tri), (int64_t)B * T, (uint32_t)F, prefix,
                                                (const int4*)rects, w.mask, w.wpre, frag_pix, (float4*)frag_attrs);
     S2C_CHECK_LAUNCH("tri_list_kernel<write>");
     return S2C_OK;

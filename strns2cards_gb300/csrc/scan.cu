@@ -12,6 +12,7 @@
 
 #include "common.cuh"
 #include "scan.cuh"
+#include "list.cuh"
 
 namespace s2c {
 
@@ -240,6 +241,37 @@ s2c_status read_count(const int64_t* d_total, int64_t* host, cudaStream_t st) {
 }  // namespace s2c
 
 using namespace s2c;
+
+namespace s2c {
+
+__global__ void popc_words_kernel(int64_t n, const uint32_t* __restrict__ mask, int32_t* __restrict__ counts) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        counts[i] = __popc(mask[i]);
+}
+
+size_t list_carve(int64_t F, void* base, size_t cap, ListWs* w) {
+    Carver cv(base, cap);
+    ListWs r;
+    const int64_t nw = std::max<int64_t>((F + 31) / 32, 1);
+    r.mask = cv.take<uint32_t>(nw);
+    r.wpre = cv.take<int32_t>(nw);
+    r.total = cv.take<int64_t>(1);
+    r.scan = cv.take<char>(scan_workspace_bytes(nw));
+    if (w) *w = r;
+    return cv.off;
+}
+
+s2c_status list_count(int64_t F, const ListWs& w, int64_t* num, cudaStream_t st) {
+    const int64_t nw = (F + 31) / 32;
+    if (nw > 0) {
+        popc_words_kernel<<<grid_for(nw, 256, (int64_t)num_sms() * 8), 256, 0, st>>>(nw, w.mask, w.wpre);
+        S2C_CHECK_LAUNCH("popc_words_kernel");
+    }
+    if (s2c_status s = inclusive_scan_i32(w.wpre, nw, w.wpre, w.scan, w.total, st)) return s;
+    return read_count(w.total, num, st);
+}
+
+}  // namespace s2c
 
 extern "C" size_t s2c_filter_valid_fragments_workspace_size(int64_t n) { return scan_workspace_bytes(n) + 256; }
 extern "C" size_t s2c_compact_valid_ints_workspace_size(int64_t n) { return scan_workspace_bytes(n) + 256; }

@@ -50,13 +50,10 @@ def dda_compute_fragments(
     slopes = torch.empty((P, 2), dtype=torch.float32, device=dev)
     spans = torch.empty((P, 4), dtype=torch.float32, device=dev)
     F = _core.dda_compute_span(edge_ids, H, W, pos, edges, prefix, slopes, spans)
-    frag_pix = torch.full((F, 3), -1, dtype=torch.int32, device=dev)
-    frag_attrs = torch.empty((F, 4), dtype=torch.float32, device=dev)
-    _core.dda_compute_fragments(prefix, edge_ids, slopes, spans, H, W, pos, edges, frag_pix, frag_attrs)
-    pix_out = torch.empty_like(frag_pix)
-    attrs_out = torch.empty_like(frag_attrs)
-    n = _core.filter_valid_fragments(frag_pix, frag_attrs, pix_out, attrs_out)
-    return pix_out[:n], attrs_out[:n]
+    # the reference writes every DDA step (-1 where rejected) and compacts the list
+    # (dda.py:50-76); here the accepted steps are counted and written straight into a list of
+    # their own: the same fragments in the same order
+    return _core.dda_compact_fragments(prefix, edge_ids, slopes, spans, H, W, pos, edges, F)
 
 
 class DDAInterpolateAttributes(torch.autograd.Function):

@@ -236,3 +236,39 @@ def test_compact_valid_ints_in_order():
     out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
     n = _core.compact_valid_ints(cu(a), out)
     assert np.array_equal(np_(out[:n]), a[a >= 0])
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_compacted_dda_fragments_equal_the_filtered_raw_list(seed):
+    """``dda_compute_fragments`` writes the accepted DDA steps straight into their own list;
+    it must equal the raw list of every step (-1 where rejected: outside the image or the
+    depth range) compacted by ``filter_valid_fragments``, in order -- with edge_ids selecting
+    views, segments leaving the image, perspective, a vertex behind the camera and an empty
+    selection."""
+    import strns2cards_gb300 as s2c
+    from strns2cards_gb300 import _core
+    rng = np.random.default_rng(seed)
+    B, V, E, H, W = 2, 900, 800, 70, 130
+    pos = rng.uniform(-1.4, 1.4, size=(B, V, 4)).astype(np.float32)
+    pos[..., 3] = rng.uniform(0.3, 1.7, size=(B, V))
+    pos[..., :2] *= pos[..., 3:4]
+    pos[..., 2] = rng.uniform(-1.3, 1.3, size=(B, V)) * pos[..., 3]     # some beyond the depth range
+    pos[0, :20, 3] = -0.5                                                # behind the camera
+    edges = np.stack([rng.integers(0, V, E), rng.integers(0, V, E)], 1).astype(np.int32)
+    ids = rng.permutation(B * E)[: B * E - 137].astype(np.int32)
+    p, e, i = cu(pos), cu(edges), cu(ids)
+    P = ids.shape[0]
+    prefix = torch.empty(P, dtype=torch.int32, device="cuda")
+    slopes = torch.empty((P, 2), dtype=torch.float32, device="cuda")
+    spans = torch.empty((P, 4), dtype=torch.float32, device="cuda")
+    F = _core.dda_compute_span(i, H, W, p, e, prefix, slopes, spans)
+    raw_p = torch.full((F, 3), -1, dtype=torch.int32, device="cuda")
+    raw_a = torch.empty((F, 4), dtype=torch.float32, device="cuda")
+    _core.dda_compute_fragments(prefix, i, slopes, spans, H, W, p, e, raw_p, raw_a)
+    out_p, out_a = torch.empty_like(raw_p), torch.empty_like(raw_a)
+    n = _core.filter_valid_fragments(raw_p, raw_a, out_p, out_a)
+    fp, fa = s2c.dda_compute_fragments((H, W), p, e, i)
+    assert F > n > 1000 and fp.shape[0] == n
+    assert torch.equal(fp, out_p[:n]) and torch.equal(fa, out_a[:n])
+    ep, ea = s2c.dda_compute_fragments((H, W), p, e, i[:0])
+    assert ep.shape == (0, 3) and ea.shape == (0, 4)
