@@ -8,6 +8,7 @@
 // compaction keeps input order, so exact depth ties resolve to the first fragment in
 // (view, triangle, row-major pixel) order, deterministically.
 #include <algorithm>
+#include <climits>
 
 #include "common.cuh"
 #include "scan.cuh"
@@ -372,14 +373,34 @@ __global__ void __launch_bounds__(256) tri_rect_area_kernel(int H, int W, int B,
         rects[idx] = rc;
         // work units of the balanced raster: runs of kRasterRun horizontally adjacent pixels
         areas[idx] = (int32_t)((uint32_t)rc.y * (((uint32_t)rc.w + (kRasterRun - 1)) / kRasterRun));
-        if (CR.r && rc.y > 0 && rc.w > 0 && t < CR.num_t2c) {
-            const int c = __ldg(CR.t2c + t);   // the raster's cluster bit for t (raster_covered)
-            if (c >= 0 && c < CR.Kp) {
-                int* q = (int*)(CR.r + (int64_t)b * CR.Kp + c);
-                atomicMin(q + 0, rc.x);
-                atomicMax(q + 1, rc.x + rc.y);
-                atomicMin(q + 2, rc.z >> 5);
-                atomicMax(q + 3, ((rc.z + rc.w - 1) >> 5) + 1);
+        if (CR.r) {
+            // the raster's cluster bit for t (raster_covered); lanes of one (view, cluster) --
+            // consecutive triangles of a card -- reduce their rectangles first, and one lane
+            // per group extends the cluster's rectangle (a card's 128 triangles would
+            // otherwise queue 128 deep on the same four words)
+            int64_t key = -1;
+            int y0 = INT_MAX, y1 = INT_MIN, q0 = INT_MAX, q1 = INT_MIN;
+            if (rc.y > 0 && rc.w > 0 && t < CR.num_t2c) {
+                const int c = __ldg(CR.t2c + t);
+                if (c >= 0 && c < CR.Kp) {
+                    key = (int64_t)b * CR.Kp + c;
+                    y0 = rc.x;
+                    y1 = rc.x + rc.y;
+                    q0 = rc.z >> 5;
+                    q1 = ((rc.z + rc.w - 1) >> 5) + 1;
+                }
+            }
+            const unsigned grp = __match_any_sync(__activemask(), key);
+            y0 = __reduce_min_sync(grp, y0);
+            y1 = __reduce_max_sync(grp, y1);
+            q0 = __reduce_min_sync(grp, q0);
+            q1 = __reduce_max_sync(grp, q1);
+            if (key >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) {
+                int* q = (int*)(CR.r + key);
+                atomicMin(q + 0, y0);
+                atomicMax(q + 1, y1);
+                atomicMin(q + 2, q0);
+                atomicMax(q + 3, q1);
             }
         }
     }
