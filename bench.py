@@ -920,7 +920,7 @@ def serving_numbers(n_jobs):
     K in {256, 1024, 4096}, 50 iterations each), HBM budget 150 GB; the same stream served
     one job at a time with plain calls is timed beside it."""
     import torch
-    from strns2cards_gb300.serving import poisson_stream, serve, serve_serial
+    from strns2cards_gb300.serving import poisson_stream, serve, serve_serial, serve_serial_dropin
     n = max(n_jobs, 4)
     reqs = poisson_stream(n, rate=20.0, seed=1)
     warm = poisson_stream(2, rate=20.0, seed=2, scale=0.05, iterations=3)
@@ -936,6 +936,14 @@ def serving_numbers(n_jobs):
     ser = serve_serial(reqs)
     wall_s = time.perf_counter() - t0
     lat_s = np.array([r.latency for r in ser])
+    # the plain per-call path (the drop-in ops as the reference's fitting loop calls them),
+    # one job at a time back to back, on the stream's first jobs
+    m = min(n, 12)
+    t0 = time.perf_counter()
+    serve_serial_dropin(reqs[:m])
+    torch.cuda.synchronize()
+    wall_d = time.perf_counter() - t0
+    iters_d = sum(r.iterations for r in reqs[:m])
     h2d = sum(r.strand_pos.nbytes + r.strand_edges.nbytes + r.strand_e2c.nbytes + r.card_pos.nbytes +
               r.card_tri.nbytes + r.card_t2c.nbytes for r in reqs)
     return dict(jobs=n, jobs_per_s=n / wall, iterations_per_s=iters / wall, wall_s=wall,
@@ -944,6 +952,10 @@ def serving_numbers(n_jobs):
                               "latency_p50_s": float(np.percentile(lat_s, 50)),
                               "latency_p99_s": float(np.percentile(lat_s, 99))},
                 served_over_serial_iterations=(iters / wall) / (iters / wall_s),
+                dropin_serial={"jobs": m, "iterations_per_s": iters_d / wall_d,
+                               "ops": "compute_fragments + cluster_mask_from_fragments, "
+                                      "antialiased_cluster_bitset_loss (XOR count) + backward, cluster_iou, step"},
+                served_over_dropin_iterations=(iters / wall) / (iters_d / wall_d),
                 h2d_bytes_per_job=h2d // n, d2h_bytes_per_job=sum(r.card_pos.nbytes for r in reqs) // n,
                 clocks=clk.summary())
 
@@ -960,7 +972,9 @@ def run_serving(args):
                                    "full-size pipeline each; HBM budget 150 GB",
                        "iterations_per_s": r["iterations_per_s"], "latency_p50_s": r["latency_p50_s"],
                        "latency_p99_s": r["latency_p99_s"], "serial_plain": r["serial_plain"],
-                       "served_over_serial_iterations": r["served_over_serial_iterations"]},
+                       "served_over_serial_iterations": r["served_over_serial_iterations"],
+                       "dropin_serial": r["dropin_serial"],
+                       "served_over_dropin_iterations": r["served_over_dropin_iterations"]},
             "e2e": {"value": r["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": r["h2d_bytes_per_job"],
                     "d2h_bytes_per_step": r["d2h_bytes_per_job"]},
             "roofline": None, "cpu_baseline": None, "clocks": r["clocks"], "gpu_launches": None}

@@ -291,6 +291,55 @@ def serve_serial(requests: List[JobSpec], device="cuda", realtime: bool = True) 
     return results
 
 
+def serve_serial_dropin(requests: List[JobSpec], device="cuda") -> List[JobResult]:
+    """The same jobs one at a time, back to back, through the drop-in ops as the reference's
+    fitting loop calls them (3_fitting.py:254-261, 381-406): the target by
+    dda_compute_fragments + cluster_mask_from_fragments, then per iteration compute_fragments
+    + cluster_mask_from_fragments, antialiased_cluster_bitset_loss (the XOR count) and its
+    gradient, the per-card IoU counts and the step.  The plain per-call baseline of the
+    served form."""
+    from .antialias import antialiased_cluster_bitset_loss
+    from .bitset_utils import cluster_iou
+    from .dda import dda_compute_fragments
+    from .rasterize import cluster_mask_from_fragments, compute_fragments
+    dev = torch.device(device)
+    results = [JobResult(r.name, r.arrival) for r in requests]
+    t0 = time.perf_counter()
+    for i, spec in enumerate(requests):
+        results[i].admitted = time.perf_counter() - t0
+        H = W = spec.res
+        K = spec.clusters
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        fp, fa = dda_compute_fragments((H, W), t(spec.strand_pos), t(spec.strand_edges))
+        target = cluster_mask_from_fragments((H, W), fp, fa, t(spec.strand_e2c), K)
+        del fp, fa
+        cpos, tri, t2c = t(spec.card_pos), t(spec.card_tri), t(spec.card_t2c)
+        edges_h, e2t_h = build_edges_from_triangles(spec.card_tri)
+        edges, e2t = t(edges_h), t(e2t_h)
+        e2c = t(spec.card_t2c[e2t_h[:, 0]].astype(np.int32))
+        losses, iou = [], None
+        for it in range(spec.iterations):
+            fp, fa = compute_fragments((H, W), cpos, tri)
+            bits = cluster_mask_from_fragments((H, W), fp, fa, t2c, K)
+            p = cpos.detach().requires_grad_(True)
+            loss = antialiased_cluster_bitset_loss(bits, target, p, tri, edges, e2t, e2c, 7.0, 0.5,
+                                                   count_xor_error=True)
+            loss.backward()
+            iou = cluster_iou(bits, target, K)[1:]
+            if it == 0:
+                results[i].iou_first_inter, results[i].iou_first_union = (x.cpu().numpy() for x in iou)
+            losses.append(loss.detach())
+            with torch.no_grad():
+                step_towards(cpos, p.grad, spec.lr, spec.res)
+        res = results[i]
+        res.card_pos = cpos.cpu().numpy()
+        res.loss = [int(x) for x in torch.stack(losses).tolist()] if losses else []
+        if iou is not None:
+            res.iou_inter, res.iou_union = (x.cpu().numpy() for x in iou)
+        res.finished = time.perf_counter() - t0
+    return results
+
+
 def poisson_stream(num_requests: int, rate: float = 20.0, seed: int = 1, scale: float = 1.0,
                    iterations: int = 50) -> List[JobSpec]:
     """Request stream: Poisson arrivals (rate per second, seed 1); strand count log-uniform in

@@ -65,3 +65,19 @@ def test_footprint_bounds_the_allocator():
         peak = torch.cuda.max_memory_allocated() - base
         assert peak <= spec.footprint(), (spec.name, peak, spec.footprint())
         del job
+
+
+def test_plain_dropin_loop_gives_the_served_results():
+    """The plain per-call baseline (the drop-in ops in the reference's fitting-loop order) and
+    the served iteration (cluster planes in rectangles) are the same iteration: first XOR loss
+    and per-card IoU counts exact, final cards to 1e-5 of their max-norm."""
+    from strns2cards_gb300.serving import serve_serial, serve_serial_dropin, synthetic_job
+    reqs = [synthetic_job(600, 16, 192, 96, seed=31, iterations=5), synthetic_job(900, 32, 128, 256, seed=32,
+                                                                                  iterations=5)]
+    served = serve_serial(reqs, realtime=False)
+    plain = serve_serial_dropin(reqs)
+    for a, b in zip(served, plain):
+        assert a.loss[0] == b.loss[0] > 0 and len(b.loss) == 5
+        assert np.array_equal(a.iou_first_inter, b.iou_first_inter)
+        assert np.array_equal(a.iou_first_union, b.iou_first_union)
+        assert close(b.card_pos, a.card_pos)
