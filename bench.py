@@ -932,6 +932,11 @@ def serving_numbers(n_jobs):
         wall = time.perf_counter() - t0
     lat = np.array([r.latency for r in res])
     iters = sum(r.iterations for r in reqs)
+    # capacity: the same jobs all waiting at the start (the GPU, not the stream, sets the rate)
+    t0 = time.perf_counter()
+    serve(reqs, 150 << 30, realtime=False)
+    torch.cuda.synchronize()
+    wall_c = time.perf_counter() - t0
     t0 = time.perf_counter()
     ser = serve_serial(reqs)
     wall_s = time.perf_counter() - t0
@@ -956,6 +961,8 @@ def serving_numbers(n_jobs):
                                "ops": "compute_fragments + cluster_mask_from_fragments, "
                                       "antialiased_cluster_bitset_loss (XOR count) + backward, cluster_iou, step"},
                 served_over_dropin_iterations=(iters / wall) / (iters_d / wall_d),
+                capacity={"jobs_per_s": n / wall_c, "iterations_per_s": iters / wall_c,
+                          "over_dropin_iterations": (iters / wall_c) / (iters_d / wall_d)},
                 h2d_bytes_per_job=h2d // n, d2h_bytes_per_job=sum(r.card_pos.nbytes for r in reqs) // n,
                 clocks=clk.summary())
 
@@ -974,7 +981,8 @@ def run_serving(args):
                        "latency_p99_s": r["latency_p99_s"], "serial_plain": r["serial_plain"],
                        "served_over_serial_iterations": r["served_over_serial_iterations"],
                        "dropin_serial": r["dropin_serial"],
-                       "served_over_dropin_iterations": r["served_over_dropin_iterations"]},
+                       "served_over_dropin_iterations": r["served_over_dropin_iterations"],
+                       "capacity_all_jobs_waiting": r["capacity"]},
             "e2e": {"value": r["jobs_per_s"], "unit": "jobs/s", "h2d_bytes_per_step": r["h2d_bytes_per_job"],
                     "d2h_bytes_per_step": r["d2h_bytes_per_job"]},
             "roofline": None, "cpu_baseline": None, "clocks": r["clocks"], "gpu_launches": None}
