@@ -59,6 +59,21 @@ def test_argument_errors_come_back_as_status_without_a_gpu(lib_built):
         ("s2c_build_edges_device", (-1, None, 4, None, None, None, None, None, 0, None)),
         ("s2c_build_edges_device", (5, None, 4, None, None, None, None, None, 0, None)),          # null counts
         ("s2c_resample_strands_by_arclength_host", (2, None, None, 1, None)),                     # target < 2
+        # compacted fragment lists
+        ("s2c_count_fragments", (0, 8, 1, 3, None, 1, None, None, None, 0, None, 0, None, None)),   # H = 0
+        ("s2c_count_fragments", (8, 8, 1, 3, None, 1, None, None, None, 1 << 31, None, 0, None, None)),
+        ("s2c_write_fragments", (8, 8, 1, 3, None, 1, None, None, None, 5, None, 0, None, None, None)),  # nulls
+        ("s2c_dda_count_fragments", (4, 10, None, None, None, None, 0, 8, 1, 2, None, 1, None, None, 0, None,
+                                     None)),                                                      # H = 0
+        ("s2c_dda_write_fragments", (4, -1, None, None, None, None, 8, 8, 1, 2, None, 1, None, None, 0, None, None,
+                                     None)),                                                      # F < 0
+        # plane rectangles
+        ("s2c_planes_clear_rects", (1, 8, 40, 1, None, None, None)),                              # nulls
+        ("s2c_planes_clear_rects", (1, 8, 40, 1, ctypes.c_void_p(16), ctypes.c_void_p(20), None)),  # misaligned rects
+        ("s2c_planes_bounds", (1, 8, 40, 0, ctypes.c_void_p(16), ctypes.c_void_p(16), None)),       # S = 0
+        ("s2c_cluster_iou_counts_planes_rects", (1, 8, 40, 1, 33, None, None, None, None, None, None, None, None)),
+        ("s2c_rasterize_fused_planes_onto", (1, 8, 8, 3, None, 1, None, None, 1, 1, None, ctypes.c_void_p(16), None,
+                                             0, None)),                                           # null planes
     ]
     for name, args in cases:
         st = getattr(L, name)(*args)
