@@ -76,10 +76,11 @@ def test_raster_onto_planes_over_iterations_equals_clearing_raster():
         p[..., :2] += rng.normal(scale=0.03, size=p[..., :2].shape).astype(np.float32)   # the cards move
 
 
-def test_planes_bounds_and_clear_rects():
+@pytest.mark.parametrize("H,W", [(37, 150), (40, 128)])   # plane words not / a multiple of 4
+def test_planes_bounds_and_clear_rects(H, W):
     from strns2cards_gb300 import _core
-    rng = np.random.default_rng(3)
-    B, H, W, S = 2, 37, 150, 2
+    rng = np.random.default_rng(3 + H)
+    B, S = 2, 2
     WQ = (W + 31) // 32
     pl = np.zeros((B, 32 * S, H, WQ), np.uint32)
     for b in range(B):
